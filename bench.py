@@ -1,0 +1,318 @@
+"""Throughput benchmark of the GPU phonon step loop: phonon-steps/s on the kinked
+three-arm structure (400 quadrilateral cells / sensors, periodic mode, dt 2 ps, 5000
+measurement steps, output every 50 steps, 1e7 phonons per step, Si-like material).
+
+A benchmark step is one complete simulation run of that model (Model::runSimulation).
+  value   phonon-steps / device time of the transport kernels, model already on the GPU
+  e2e     the same through the public C ABI call (psim_model_run on a freshly loaded model,
+          results read back to the host), host<->device copies inside the timed region
+Phonon-steps are counted by the kernels (phonons alive at a measurement boundary).
+
+"1e7 phonons per step" is a steady population; psim's input takes a total phonon budget,
+so the budget is num_phonons = 1e7 * steps / L with L the mean lifetime in steps measured
+by an untimed pilot run of the same model.
+
+--impl reference times the CPU oracle (the reference algorithm restated in C++, bit-exact
+with the reference on the same seed) on a bounded sample of the same model with every host
+thread.  Under torchrun each rank simulates its own phonons (weak scaling: the rank's seed
+selects its share of the random streams); the tallies are summed once per run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PER_STEP = 1.0e7
+STEPS = 5000
+DT_PS = 2.0
+BYTES_PER_PHONON_STEP = 64  # one 32-byte state record read and one written
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def reduce_max(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def model_json(path: str, num_phonons: int, steps: int = STEPS) -> str:
+    from psim_gb300 import modelgen as mg
+    m = mg.kinked(seed=0, num_phonons=int(num_phonons), num_measurements=steps, sim_time=steps * DT_PS * 1e-3,
+                  step_interval=50)
+    return mg.write(m, path)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, out_path: str):
+        self.out_path = out_path
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.out_path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def stop(self, gpu_index: int = 0) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.out_path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(path_dir: str, budget: int, threads: int, seed: int):
+    """The oracle on a bounded sample of the workload (same model, smaller phonon budget)."""
+    from oracle import oracle
+    oracle.build()
+    p = model_json(os.path.join(path_dir, "kinked_sample.json"), budget)
+    r = oracle.run(p, seed, threads=threads)
+    return r.phonon_steps, r.seconds
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference algorithm (CPU oracle) on every host thread."""
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    budget = args.cpu_budget
+    with tempfile.TemporaryDirectory() as td:
+        for _ in range(args.warmup):
+            cpu_sample(td, budget, threads, 7)
+        steps = 0
+        secs = 0.0
+        for k in range(args.steps):
+            n, s = cpu_sample(td, budget, threads, 100 + k)
+            steps += n
+            secs += s
+    rate = steps / secs
+    src = "oracle/_ref (the reference built from source)" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "ref_driver")) else "oracle port"
+    line = {
+        "impl": "reference", "metric": "phonon-steps/s", "value": rate, "unit": "phonon-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "kinked 3-arm, 400 cells/sensors, periodic, dt 2 ps, 5000 steps",
+                   "num_phonons": budget, "sample": f"budget {budget} phonons (bounded CPU sample)"},
+        "cpu_baseline": {"value": rate, "unit": "phonon-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"kinked model, 5000 steps, {budget}-phonon budget per run; {src} is not available "
+                                   f"on this host, the bit-exact C++ restatement (oracle/) runs instead"},
+        "e2e": {"value": rate, "unit": "phonon-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--per-step", type=float, default=PER_STEP)
+    ap.add_argument("--measurements", type=int, default=STEPS)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--cpu-budget", type=int, default=200000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    from psim_gb300 import api, build
+    build.build()
+    precision = api.FP64 if args.precision == "fp64" else api.FP32
+    steps_n = args.measurements
+    td = tempfile.mkdtemp(prefix="psim_bench_")
+
+    # pilot run (untimed): mean lifetime in steps -> phonon budget for the target population
+    pilot = api.Model(model_json(os.path.join(td, "pilot.json"), 200000, steps_n))
+    pilot.run(seed=99 + rank, precision=precision)
+    pc = pilot.counters()
+    lifetime = pc["phonon_steps"] / max(pc["phonons"], 1)
+    budget = int(args.per_step * steps_n / lifetime)
+    path = model_json(os.path.join(td, "kinked.json"), budget, steps_n)
+    model = api.Model(path)
+
+    stream = torch.cuda.Stream()
+    for w in range(args.warmup):
+        model.run(seed=1000 * (rank + 1) + w, precision=precision, stream=stream.cuda_stream)
+
+    # ---- timed: device-resident runs
+    clocks = ClockSampler(os.path.join(td, "clocks.csv"))
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    phonon_steps = 0
+    kernel_ms = 0.0
+    launches = 0
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for k in range(args.steps):
+        model.run(seed=7000 * (rank + 1) + k, precision=precision, stream=stream.cuda_stream)
+        c = model.counters()
+        phonon_steps += c["phonon_steps"]
+        kernel_ms += c["kernel_ms"]
+        launches += c["kernel_launches"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop(local)
+    barrier(dist)
+    span_ms = ev0.elapsed_time(ev1)
+    kernel_s = reduce_max(dist, kernel_ms / 1e3)
+    total_steps = reduce_sum(dist, float(phonon_steps))
+    value = total_steps / kernel_s
+    ms_per_step = 1e3 * reduce_max(dist, span_ms / 1e3) / args.steps
+
+    # roofline of the dominant kernel (the FP32/FP64 transport step)
+    per_launch_bytes = phonon_steps / launches * BYTES_PER_PHONON_STEP * (2 if precision == api.FP64 else 1)
+    avg_launch_s = kernel_ms / 1e3 / launches
+    peak, peak_kind = peaks()
+    achieved = per_launch_bytes / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_source": f"{peak_kind} hbm_gbs", "kernel": "step_kernel_" + args.precision,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "avg_launch_us": avg_launch_s * 1e6}
+    profile = os.path.join(ROOT, "profiles", f"traffic_step_kernel_{args.precision}_kinked.json")
+    if os.path.exists(profile):
+        tr = json.load(open(profile))
+        roofline["traffic"] = tr.get("dram_bytes_per_phonon_step", 0) * phonon_steps / launches
+        roofline["traffic_source"] = tr.get("source")
+
+    # ---- e2e through the public C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        barrier(dist)
+        e_steps = 0
+        h2d = d2h = 0
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            m = api.Model(path)
+            m.run(seed=9000 * (rank + 1) + k, precision=precision)
+            stats = m.measurements()
+            temps, fluxes = m.series(0)
+            c = m.counters()
+            e_steps += c["phonon_steps"]
+            h2d += c["h2d_bytes"]
+            d2h += c["d2h_bytes"] + stats.nbytes + temps.nbytes + fluxes.nbytes
+            m.close()
+        e_wall = time.perf_counter() - t0
+        barrier(dist)
+        e_wall = reduce_max(dist, e_wall)
+        e_total = reduce_sum(dist, float(e_steps))
+        e2e = {"value": e_total / e_wall, "unit": "phonon-steps/s", "h2d_bytes_per_step": int(h2d / args.steps),
+               "d2h_bytes_per_step": int(d2h / args.steps)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        n, s = cpu_sample(td, args.cpu_budget, threads, 5)
+        cpu = {"value": n / s, "unit": "phonon-steps/s", "cores": threads, "kind": "port",
+               "sample": f"kinked model, {steps_n} steps, {args.cpu_budget}-phonon budget ({n} phonon-steps, {s:.1f} s) "
+                         f"on {threads} host threads with the CPU oracle"}
+
+    if rank == 0:
+        line = {
+            "metric": "phonon-steps/s", "value": value, "unit": "phonon-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == api.FP32 else "f64",
+            "data": "synthetic",
+            "config": {"workload": "kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt 2 ps, "
+                                   f"{steps_n} steps, output every 50 steps, {args.per_step:.0e} phonons per step",
+                       "num_phonons_per_rank": budget, "mean_lifetime_steps": lifetime,
+                       "mean_population": phonon_steps / args.steps / steps_n,
+                       "l2": "inputs larger than L2 (phonon state 2 x 32 B x population)",
+                       "precision": args.precision, "bench_step": "one full simulation run"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
+            "clocks": clk, "wall_s_timed": wall,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

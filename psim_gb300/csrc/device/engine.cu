@@ -1,0 +1,648 @@
+// GPU engine: device model construction, phonon births, the per-step launch sequence
+// (captured as one CUDA graph per run) and tally read-out.
+#include "engine.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../host/geom64.hpp"
+#include "common.cuh"
+
+namespace psim::gpu {
+
+void launch_step_f32(const StepParams& P, int grid, cudaStream_t stream);
+void launch_step_f64(const StepParams& P, int grid, cudaStream_t stream);
+int occupancy_f32();
+int occupancy_f64();
+void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
+                      double* stats_h, cudaStream_t stream);
+void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream);
+
+namespace {
+
+void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) { throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e)); }
+}
+
+struct Buf {
+    void* p{ nullptr };
+    std::size_t bytes{ 0 };
+    Buf() = default;
+    ~Buf() { release(); }
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
+    void alloc(std::size_t n) {
+        release();
+        bytes = n > 0 ? n : 16;
+        check(cudaMalloc(&p, bytes), "cudaMalloc");
+    }
+    void release() {
+        if (p != nullptr) { cudaFree(p); }
+        p = nullptr;
+        bytes = 0;
+    }
+    template<typename T> void upload(const std::vector<T>& v) {
+        alloc(v.size() * sizeof(T));
+        if (!v.empty()) { check(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload"); }
+    }
+    template<typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+Line64 line64(psim::P2 a, psim::P2 b) {
+    const psim::Seg64 s = psim::make_seg(a, b, nullptr);
+    return Line64{ s.a.x, s.a.y, s.b.x, s.b.y, s.m, s.c, s.lo.x, s.lo.y, s.hi.x, s.hi.y };
+}
+
+psim::Seg64 seg_from(const double* l) { return psim::make_seg(psim::P2{ l[0], l[1] }, psim::P2{ l[2], l[3] }, nullptr); }
+
+// Walker alias table (Vose's construction) over the (bin, polarization) outcomes that
+// Material::freqIndex (psim/src/material.cpp:64-75) produces from a cumulative table: the
+// bisection returns bin h with probability cum[h] - cum[h-1] (bin 1 also takes bin 0's mass,
+// bin 999 everything above cum[998]) and LA with probability la_frac[h] (TA when it is NaN).
+std::vector<std::uint32_t> alias_table(const double* tab) {
+    std::vector<double> p(kAliasCols, 0.);
+    for (int h = 1; h < kBins; ++h) {
+        const double cum_h = tab[2 * h];
+        const double prev = (h == 1) ? 0. : tab[2 * (h - 1)];
+        double ph = (h == kBins - 1) ? 1. - prev : cum_h - prev;
+        if (!(ph > 0.)) { ph = 0.; }
+        double la = tab[2 * h + 1];
+        if (std::isnan(la)) { la = 0.; }
+        la = std::min(std::max(la, 0.), 1.);
+        p[2 * h] = ph * la;
+        p[2 * h + 1] = ph * (1. - la);
+    }
+    double total = 0.;
+    for (double v : p) { total += v; }
+    if (!(total > 0.)) { throw std::invalid_argument("frequency table has no probability mass"); }
+    std::vector<double> q(kAliasCols);
+    std::vector<int> small;
+    std::vector<int> large;
+    for (int i = 0; i < kAliasCols; ++i) {
+        q[i] = p[i] / total * kAliasCols;
+        (q[i] < 1. ? small : large).push_back(i);
+    }
+    std::vector<std::uint32_t> out(kAliasCols);
+    constexpr double kOne = 2097152.;// 2^21
+    while (!small.empty() && !large.empty()) {
+        const int l = small.back();
+        small.pop_back();
+        const int g = large.back();
+        large.pop_back();
+        const auto thr = static_cast<std::uint32_t>(std::min(std::floor(q[l] * kOne + 0.5), kOne - 1.));
+        out[l] = (thr << 11) | static_cast<std::uint32_t>(g);
+        q[g] = (q[g] + q[l]) - 1.;
+        (q[g] < 1. ? small : large).push_back(g);
+    }
+    // Rounding leftovers: columns of real outcomes keep themselves; a column without
+    // probability (padding, or an impossible outcome) always takes the most probable outcome.
+    const int best = static_cast<int>(std::max_element(p.begin(), p.end()) - p.begin());
+    for (int i : large) { out[i] = (0x1FFFFFU << 11) | static_cast<std::uint32_t>(i); }
+    for (int i : small) {
+        out[i] = p[i] > 0. ? ((0x1FFFFFU << 11) | static_cast<std::uint32_t>(i)) : static_cast<std::uint32_t>(best);
+    }
+    for (int i = 2 * kBins; i < kAliasCols; ++i) {// padding columns must never be accepted
+        if ((out[i] >> 11) != 0U || (out[i] & 0x7FFU) >= static_cast<std::uint32_t>(2 * kBins)) { out[i] = static_cast<std::uint32_t>(best); }
+    }
+    return out;
+}
+
+__global__ void unpack_kernel(const TallySlot* t, std::uint32_t S, std::uint64_t K, long long* energy, double* flux) {
+    const std::uint64_t n = static_cast<std::uint64_t>(S) * K;
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x) {
+        const std::uint64_t k = i / S;
+        const std::uint32_t s = static_cast<std::uint32_t>(i % S);
+        const TallySlot v = t[i];
+        energy[s * K + k] = v.count;
+        flux[(s * K + k) * 2] = static_cast<double>(v.fx) * kFluxScaleInv;
+        flux[(s * K + k) * 2 + 1] = static_cast<double>(v.fy) * kFluxScaleInv;
+    }
+}
+
+}// namespace
+
+struct Engine::Impl {
+    Buf cells32, cells64, subs64, sensors, materials, emitters, alias, centre32, vel32, centre64, vel64;
+    std::vector<EmitterDev> emit_host;
+    std::vector<BirthGroup> groups;
+    std::vector<std::uint32_t> group_begin;// [N+1]
+    std::vector<std::uint32_t> n_new;      // [N]
+    std::vector<std::uint32_t> id_base;    // [N]
+    Buf d_groups;
+    Buf state[2];
+    std::uint64_t capacity{ 0 };
+    Buf counts;  // 3 x u32
+    Buf counters;// 8 x u64: phonon-steps, relocations, overflow, max population, event-limit hits
+    Buf tally;   // [K][S]
+    Buf unpacked_energy, unpacked_flux;
+    std::uint64_t total{ 0 };
+    std::uint32_t key0{ 0 }, key1{ 0 };
+    bool builders_ready{ false };
+    cudaEvent_t ev0{ nullptr }, ev1{ nullptr };
+    cudaStream_t own{ nullptr };
+    int sms{ 0 };
+};
+
+int device_count() noexcept {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+Engine::Engine(const SimDesc& d)
+    : desc_{ d }
+    , impl_{ std::make_unique<Impl>() } {
+    if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
+    if (d.n_cells == 0 || d.n_sensors == 0 || d.n_materials == 0 || d.steps == 0) { throw std::invalid_argument("empty model"); }
+    if (d.n_materials > kMaxMaterials) { throw std::invalid_argument("at most 16 materials are supported"); }
+    if (d.n_cells >= (1U << 24)) { throw std::invalid_argument("at most 2^24 - 1 cells are supported"); }
+    if (d.steps >= 0xFFFFFFFFULL) { throw std::invalid_argument("too many measurement steps"); }
+    Impl& I = *impl_;
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&I.sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    check(cudaStreamCreateWithFlags(&I.own, cudaStreamNonBlocking), "stream");
+    stream_ = I.own;
+    check(cudaEventCreate(&I.ev0), "event");
+    check(cudaEventCreate(&I.ev1), "event");
+
+    const std::uint32_t C = d.n_cells;
+    // ---- cells
+    std::vector<CellF32> c32(C);
+    std::vector<CellF64> c64(C);
+    std::vector<Sub64> subs(d.sub_kind.size());
+    auto vtx = [&](std::uint32_t c, int i) {
+        return psim::P2{ d.cell_vertices[6 * c + 2 * i], d.cell_vertices[6 * c + 2 * i + 1] };
+    };
+    std::vector<int> cell_sign(C);
+    for (std::uint32_t c = 0; c < C; ++c) {
+        cell_sign[c] = psim::tri_clockwise(vtx(c, 0), vtx(c, 1), vtx(c, 2)) ? 1 : -1;
+    }
+    for (std::uint32_t c = 0; c < C; ++c) {
+        CellF32& f = c32[c];
+        CellF64& g = c64[c];
+        std::memset(&f, 0, sizeof f);
+        std::memset(&g, 0, sizeof g);
+        const psim::P2 o = vtx(c, 0);
+        const std::uint32_t sensor = d.cell_sensor[c];
+        if (sensor >= d.n_sensors) { throw std::invalid_argument("cell sensor index out of range"); }
+        f.sensor = g.sensor = sensor;
+        f.material = g.material = d.sensor_material[sensor];
+        const double spec = std::min(std::max(d.cell_spec[c], 0.), 1.);
+        f.spec = static_cast<float>(spec);
+        g.spec = spec;
+        f.rev = 0;
+        for (int e = 0; e < 3; ++e) {
+            const psim::P2 a = vtx(c, e);
+            const psim::P2 b = vtx(c, (e + 1) % 3);
+            f.vert[e] = make_float2(static_cast<float>(a.x - o.x), static_cast<float>(a.y - o.y));
+            g.vx[e] = a.x;
+            g.vy[e] = a.y;
+            g.edge[e] = line64(a, b);
+            const psim::P2 n_in = psim::seg_normal(a, b, cell_sign[c]);
+            g.nx[e] = n_in.x;
+            g.ny[e] = n_in.y;
+            const double h = -(n_in.x * (a.x - o.x) + n_in.y * (a.y - o.y));
+            f.edge[e] = make_float4(static_cast<float>(-n_in.x), static_cast<float>(-n_in.y), static_cast<float>(h),
+                                    static_cast<float>(psim::dist2(a, b)));
+            const std::uint32_t sb = d.edge_sub_begin[3 * c + e];
+            const std::uint32_t se = d.edge_sub_begin[3 * c + e + 1];
+            g.sub_begin[e] = sb;
+            if (e == 2) { g.sub_begin[3] = se; }
+            int link = -1;
+            std::uint32_t rev = kNoEdge;
+            bool flip = false;
+            for (std::uint32_t k = sb; k < se && link == -1; ++k) {
+                if (d.sub_kind[k] != 0) { continue; }
+                const std::uint32_t n = d.sub_target[k];
+                if (n >= C) { throw std::invalid_argument("transition target out of range"); }
+                link = static_cast<int>(n);
+                const psim::P2 on = vtx(n, 0);
+                f.offset[e] = make_float2(static_cast<float>(o.x - on.x), static_cast<float>(o.y - on.y));
+                const psim::Seg64 sl = seg_from(&d.sub_line[4 * k]);
+                const psim::P2 mid{ (sl.a.x + sl.b.x) / 2., (sl.a.y + sl.b.y) / 2. };
+                for (int e2 = 0; e2 < 3 && rev == kNoEdge; ++e2) {
+                    const psim::Seg64 ne = psim::make_seg(vtx(n, e2), vtx(n, (e2 + 1) % 3), nullptr);
+                    if (psim::on_line(ne, mid) && psim::on_line(ne, sl.a) && psim::on_line(ne, sl.b)) { rev = static_cast<std::uint32_t>(e2); }
+                }
+                const psim::P2 sn = psim::seg_normal(sl.a, sl.b, cell_sign[c]);
+                flip = (sn.x * n_in.x + sn.y * n_in.y) < 0.;
+            }
+            for (std::uint32_t k = sb; k < se && link == -1; ++k) {
+                if (d.sub_kind[k] != 1) { continue; }
+                if (d.sub_target[k] >= d.n_emitters) { throw std::invalid_argument("emitter index out of range"); }
+                link = -static_cast<int>(d.sub_target[k]) - 2;
+            }
+            f.link[e] = link;
+            f.rev |= (rev & 3U) << (2 * e);
+            if (flip) { f.rev |= 1U << (8 + e); }
+            for (std::uint32_t k = sb; k < se; ++k) {
+                Sub64& s = subs[k];
+                const double* l = &d.sub_line[4 * k];
+                s.line = line64(psim::P2{ l[0], l[1] }, psim::P2{ l[2], l[3] });
+                const psim::P2 sn = (d.sub_kind[k] == 0) ? psim::seg_normal(psim::P2{ l[0], l[1] }, psim::P2{ l[2], l[3] }, cell_sign[c]) : n_in;
+                s.nx = sn.x;
+                s.ny = sn.y;
+                s.kind = d.sub_kind[k];
+                s.target = d.sub_target[k];
+            }
+        }
+    }
+    I.cells32.upload(c32);
+    I.cells64.upload(c64);
+    I.subs64.upload(subs);
+
+    // ---- materials
+    std::vector<MaterialDev> mats(d.n_materials);
+    std::vector<float> centre32(static_cast<std::size_t>(d.n_materials) * kBins);
+    std::vector<float> vel32(static_cast<std::size_t>(d.n_materials) * 2 * kBins);
+    for (std::uint32_t m = 0; m < d.n_materials; ++m) {
+        const double* pr = &d.mat_params[8 * m];
+        MaterialDev& md = mats[m];
+        md.b_l = pr[0];
+        md.b_tn = pr[1];
+        md.b_tu = pr[2];
+        md.b_i = pr[3];
+        md.w = pr[4];
+        md.width64 = pr[5];
+        md.w_max_la64 = pr[6];
+        md.w_max_ta64 = pr[7];
+        md.cL = static_cast<float>(pr[0] * 1e26);
+        md.cTN = static_cast<float>(pr[1] * 1e13);
+        md.cTU = static_cast<float>(pr[2] * 1e26);
+        md.cI = static_cast<float>(pr[3] * 1e52);
+        md.w_cut = static_cast<float>(pr[4] / 1e13);
+        md.width = static_cast<float>(pr[5] / 1e13);
+        md.w_max_la = static_cast<float>(pr[6] / 1e13);
+        md.w_max_ta = static_cast<float>(pr[7] / 1e13);
+        for (int b = 0; b < kBins; ++b) {
+            centre32[m * kBins + b] = static_cast<float>(d.mat_freq[m * kBins + b] / 1e13);
+            vel32[(m * 2) * kBins + b] = static_cast<float>(d.mat_vel[(m * 2) * kBins + b]);
+            vel32[(m * 2 + 1) * kBins + b] = static_cast<float>(d.mat_vel[(m * 2 + 1) * kBins + b]);
+        }
+    }
+    I.materials.upload(mats);
+    I.centre32.upload(centre32);
+    I.vel32.upload(vel32);
+    I.centre64.upload(d.mat_freq);
+    I.vel64.upload(d.mat_vel);
+
+    // ---- alias tables
+    std::vector<std::uint32_t> alias(static_cast<std::size_t>(d.n_tables) * kAliasCols);
+    for (std::uint32_t t = 0; t < d.n_tables; ++t) {
+        const auto a = alias_table(&d.tables[static_cast<std::size_t>(t) * kBins * 2]);
+        std::copy(a.begin(), a.end(), alias.begin() + static_cast<std::ptrdiff_t>(t) * kAliasCols);
+    }
+    I.alias.upload(alias);
+
+    // ---- sensors
+    std::vector<SensorDev> sens(d.n_sensors);
+    constexpr double kHbar = 1.054517e-34;
+    constexpr double kBoltz = 1.38065e-23;
+    for (std::uint32_t s = 0; s < d.n_sensors; ++s) {
+        const double T = d.sensor_temp[s];
+        SensorDev& sd = sens[s];
+        sd.T = T;
+        sd.T3 = static_cast<float>(T * T * T);
+        sd.T4 = static_cast<float>(T * T * T * T);
+        sd.xk = static_cast<float>(kHbar * 1e13 / (kBoltz * T));
+        sd.material = d.sensor_material[s];
+        if (sd.material >= d.n_materials) { throw std::invalid_argument("sensor material out of range"); }
+        sd.base_table = d.sensor_base_table[s];
+        sd.scatter_table = d.sensor_scatter_table[s];
+        if (sd.base_table >= d.n_tables || sd.scatter_table >= d.n_tables) { throw std::invalid_argument("sensor table out of range"); }
+    }
+    I.sensors.upload(sens);
+
+    // ---- emitters
+    const double dt = d.sim_time / static_cast<double>(d.steps);
+    I.emit_host.resize(d.n_emitters);
+    for (std::uint32_t e = 0; e < d.n_emitters; ++e) {
+        EmitterDev& em = I.emit_host[e];
+        std::memset(&em, 0, sizeof em);
+        const std::uint32_t c = d.emit_cell[e];
+        const int edge = static_cast<int>(d.emit_edge[e]);
+        if (c >= C || edge > 2) { throw std::invalid_argument("emitter cell/edge out of range"); }
+        const psim::P2 o = vtx(c, 0);
+        const double* l = &d.emit_line[4 * e];
+        em.ax = l[0];
+        em.ay = l[1];
+        em.bx = l[2];
+        em.by = l[3];
+        em.a = make_float2(static_cast<float>(l[0] - o.x), static_cast<float>(l[1] - o.y));
+        em.b = make_float2(static_cast<float>(l[2] - o.x), static_cast<float>(l[3] - o.y));
+        em.nx64 = c64[c].nx[edge];
+        em.ny64 = c64[c].ny[edge];
+        em.nx = static_cast<float>(em.nx64);
+        em.ny = static_cast<float>(em.ny64);
+        em.cell = c;
+        em.edge = static_cast<std::uint32_t>(edge);
+        em.table = d.emit_table[e];
+        if (em.table >= d.n_tables) { throw std::invalid_argument("emit table out of range"); }
+        em.spec = c64[c].spec;
+        // EmitSurface::handlePhonon absorbs when the phonon's step time s*dt is inside
+        // [start, start + duration - dt] (psim/src/surface.cpp:61-65), evaluated exactly.
+        em.absorb_lo = 1U;
+        em.absorb_hi = 0U;
+        bool any = false;
+        for (std::uint64_t s = 0; s < d.steps; ++s) {
+            const double pt = static_cast<double>(s) * dt;
+            const bool absorb = !(pt < d.emit_start[e] || pt + dt > d.emit_start[e] + d.emit_duration[e]);
+            if (absorb) {
+                if (!any) { em.absorb_lo = static_cast<std::uint32_t>(s); }
+                em.absorb_hi = static_cast<std::uint32_t>(s);
+                any = true;
+            }
+        }
+    }
+    I.emitters.upload(I.emit_host);
+
+    model_bytes_ = I.cells32.bytes + I.cells64.bytes + I.subs64.bytes + I.materials.bytes + I.centre32.bytes + I.vel32.bytes
+                   + I.centre64.bytes + I.vel64.bytes + I.alias.bytes + I.sensors.bytes + I.emitters.bytes;
+    // ---- run buffers
+    I.counts.alloc(4 * sizeof(std::uint32_t));
+    I.counters.alloc(8 * sizeof(unsigned long long));
+    I.tally.alloc(static_cast<std::size_t>(d.recorded) * d.n_sensors * sizeof(TallySlot));
+    check(cudaMemset(I.tally.p, 0, I.tally.bytes), "memset tally");
+}
+
+Engine::~Engine() {
+    if (impl_) {
+        if (impl_->ev0 != nullptr) { cudaEventDestroy(impl_->ev0); }
+        if (impl_->ev1 != nullptr) { cudaEventDestroy(impl_->ev1); }
+        if (impl_->own != nullptr) { cudaStreamDestroy(impl_->own); }
+    }
+}
+
+std::uint64_t Engine::init_builders(double t_eq, double eff_energy, const double* cell_energy, const double* emit_energy,
+                                    const double* sensor_init_temp, std::uint64_t seed) {
+    Impl& I = *impl_;
+    const SimDesc& d = desc_;
+    const std::uint64_t N = d.steps;
+    std::mt19937_64 rng(seed ^ 0x5DEECE66DULL);
+    std::uniform_real_distribution<double> uni(0., 1.);
+    // floor(E / eff) plus one with probability equal to the fraction (modelSimulator.cpp:44-49)
+    auto count = [&](double energy) -> std::uint64_t {
+        if (!(energy > 0.) || !(eff_energy > 0.)) { return 0; }
+        double whole = 0.;
+        const double frac = std::modf(energy / eff_energy, &whole);
+        auto n = static_cast<std::uint64_t>(whole);
+        return (uni(rng) < frac) ? n + 1 : n;
+    };
+    std::vector<std::vector<BirthGroup>> per_step(N);
+    std::uint64_t total = 0;
+    std::uint32_t first0 = 0;
+    for (std::uint32_t c = 0; c < d.n_cells; ++c) {
+        const std::uint64_t n = count(cell_energy[c]);
+        if (n == 0) { continue; }
+        BirthGroup g{};
+        g.first = first0;
+        g.source = static_cast<std::int32_t>(c);
+        g.sign = (sensor_init_temp[d.cell_sensor[c]] > t_eq) ? 1 : -1;
+        per_step[0].push_back(g);
+        total += n;
+        if (total >= 0xFFFFFFFFULL) { throw std::length_error("more than 2^32 - 1 phonons in one run"); }
+        first0 += static_cast<std::uint32_t>(n);
+    }
+    std::vector<std::uint64_t> step_total(N, 0);
+    step_total[0] = first0;
+    const double dt = d.sim_time / static_cast<double>(N);
+    for (std::uint32_t e = 0; e < d.n_emitters; ++e) {
+        std::uint64_t n = count(emit_energy[e]);
+        if (n == 0) { continue; }
+        total += n;
+        if (total >= 0xFFFFFFFFULL) { throw std::length_error("more than 2^32 - 1 phonons in one run"); }
+        // Birth times are uniform over [start, start + duration] (EmitSurface::getPhononTime,
+        // psim/src/surface.cpp:67-69); the number born in each step is multinomial.
+        const double start = d.emit_start[e];
+        const double end = start + d.emit_duration[e];
+        const auto s_first = static_cast<std::uint64_t>(std::min<double>(std::floor(start / dt), static_cast<double>(N - 1)));
+        const auto s_last = static_cast<std::uint64_t>(std::min<double>(std::floor(end / dt), static_cast<double>(N - 1)));
+        double mass = end - start;
+        const int sign = (d.emit_temp[e] > t_eq) ? 1 : -1;
+        for (std::uint64_t s = s_first; s <= s_last && n > 0; ++s) {
+            const double lo = std::max(start, static_cast<double>(s) * dt);
+            const double hi = (s == s_last) ? end : std::min(end, static_cast<double>(s + 1) * dt);
+            const double len = std::max(hi - lo, 0.);
+            std::uint64_t m = n;
+            if (s != s_last) {
+                const double p = mass > 0. ? std::min(std::max(len / mass, 0.), 1.) : 1.;
+                std::binomial_distribution<std::uint64_t> bin(n, p);
+                m = bin(rng);
+            }
+            mass -= len;
+            n -= m;
+            if (m == 0) { continue; }
+            BirthGroup g{};
+            g.first = static_cast<std::uint32_t>(step_total[s]);
+            g.source = -static_cast<std::int32_t>(e) - 1;
+            g.t0_64 = lo - static_cast<double>(s) * dt;
+            g.span64 = len;
+            g.t0 = static_cast<float>(g.t0_64);
+            g.span = static_cast<float>(g.span64);
+            g.sign = sign;
+            per_step[s].push_back(g);
+            step_total[s] += m;
+        }
+    }
+    I.groups.clear();
+    I.group_begin.assign(N + 1, 0);
+    I.n_new.assign(N, 0);
+    I.id_base.assign(N, 0);
+    std::uint64_t ids = 0;
+    for (std::uint64_t s = 0; s < N; ++s) {
+        I.group_begin[s] = static_cast<std::uint32_t>(I.groups.size());
+        for (const auto& g : per_step[s]) { I.groups.push_back(g); }
+        I.n_new[s] = static_cast<std::uint32_t>(step_total[s]);
+        I.id_base[s] = static_cast<std::uint32_t>(ids);
+        ids += step_total[s];
+    }
+    I.group_begin[N] = static_cast<std::uint32_t>(I.groups.size());
+    I.d_groups.upload(I.groups);
+    counters_.h2d_bytes += I.groups.size() * sizeof(BirthGroup);
+    I.total = total;
+    I.key0 = static_cast<std::uint32_t>(seed) ^ 0x243F6A88U;
+    I.key1 = static_cast<std::uint32_t>(seed >> 32) ^ 0x85A308D3U;
+    I.builders_ready = true;
+    counters_.phonons = total;
+    return total;
+}
+
+void Engine::run(int precision, void* stream_ptr) {
+    Impl& I = *impl_;
+    const SimDesc& d = desc_;
+    if (!I.builders_ready) { throw std::logic_error("init_builders must be called before run"); }
+    cudaStream_t stream = stream_ptr != nullptr ? static_cast<cudaStream_t>(stream_ptr) : I.own;
+    const bool fp64 = precision != 0;
+    const std::size_t rec_bytes = fp64 ? 64 : 32;
+    // Capacity: the population never exceeds the number of phonons created in the run.
+    std::uint64_t want = std::max<std::uint64_t>(I.total + 1024, 4096);
+    std::size_t free_b = 0;
+    std::size_t total_b = 0;
+    check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const std::uint64_t limit = static_cast<std::uint64_t>(free_b * 0.8) / (2 * rec_bytes);
+    if (want > limit) { want = limit; }
+    if (I.capacity < want || I.state[0].bytes < want * rec_bytes) {
+        I.state[0].alloc(want * rec_bytes);
+        I.state[1].alloc(want * rec_bytes);
+        I.capacity = want;
+    }
+    check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
+    check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
+
+    StepParams P{};
+    P.cells32 = I.cells32.as<CellF32>();
+    P.cells64 = I.cells64.as<CellF64>();
+    P.subs64 = I.subs64.as<Sub64>();
+    P.sensors = I.sensors.as<SensorDev>();
+    P.materials = I.materials.as<MaterialDev>();
+    P.emitters = I.emitters.as<EmitterDev>();
+    P.alias = I.alias.as<std::uint32_t>();
+    P.centre32 = I.centre32.as<float>();
+    P.vel32 = I.vel32.as<float>();
+    P.centre64 = I.centre64.as<double>();
+    P.vel64 = I.vel64.as<double>();
+    P.n_sensors = d.n_sensors;
+    P.groups = I.d_groups.as<BirthGroup>();
+    P.capacity = static_cast<std::uint32_t>(std::min<std::uint64_t>(I.capacity, 0xFFFFFFFFULL));
+    P.n_steps = static_cast<std::uint32_t>(d.steps);
+    P.step_adj = static_cast<std::uint32_t>(d.step_adj);
+    P.n_recorded = static_cast<std::uint32_t>(d.recorded);
+    P.dt64 = d.sim_time / static_cast<double>(d.steps);
+    P.dt = static_cast<float>(P.dt64);
+    P.phasor_sim = d.phasor ? 1 : 0;
+    P.full_sim = d.full ? 1 : 0;
+    P.key0 = I.key0;
+    P.key1 = I.key1;
+    P.tally = I.tally.as<TallySlot>();
+    P.counters = I.counters.as<unsigned long long>();
+    auto* counts = I.counts.as<std::uint32_t>();
+    const int occ = std::max(1, fp64 ? occupancy_f64() : occupancy_f32());
+    int grid = grid_override_ > 0 ? grid_override_ : I.sms * occ;
+    if (const char* g = std::getenv("PSIM_GB300_GRID"); g != nullptr && std::atoi(g) > 0) { grid = std::atoi(g); }// launch-shape override
+
+    auto enqueue = [&]() {
+        for (std::uint64_t s = 0; s < d.steps; ++s) {
+            P.step = static_cast<std::uint32_t>(s);
+            P.in = I.state[s % 2].p;
+            P.out = I.state[(s + 1) % 2].p;
+            P.count_in = counts + (s % 3);
+            P.count_out = counts + ((s + 1) % 3);
+            P.count_clear = counts + ((s + 2) % 3);
+            P.group_begin = I.group_begin[s];
+            P.group_end = I.group_begin[s + 1];
+            P.n_new = I.n_new[s];
+            P.id_base = I.id_base[s];
+            if (fp64) {
+                launch_step_f64(P, grid, stream);
+            } else {
+                launch_step_f32(P, grid, stream);
+            }
+        }
+    };
+
+    check(cudaEventRecord(I.ev0, stream), "event record");
+    if (use_graph_) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        enqueue();
+        check(cudaStreamEndCapture(stream, &graph), "end capture");
+        check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+        check(cudaGraphLaunch(exec, stream), "graph launch");
+        check(cudaEventRecord(I.ev1, stream), "event record");
+        check(cudaStreamSynchronize(stream), "run sync");
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+    } else {
+        enqueue();
+        check(cudaGetLastError(), "step launch");
+        check(cudaEventRecord(I.ev1, stream), "event record");
+        check(cudaStreamSynchronize(stream), "run sync");
+    }
+    float ms = 0.f;
+    check(cudaEventElapsedTime(&ms, I.ev0, I.ev1), "event time");
+    unsigned long long c[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    check(cudaMemcpy(c, I.counters.p, sizeof c, cudaMemcpyDeviceToHost), "counters");
+    counters_.phonon_steps += c[0];
+    counters_.relocations += c[1];
+    counters_.event_limits += c[4];
+    counters_.overflow += c[2];
+    counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
+    counters_.kernel_ms += ms;
+    counters_.d2h_bytes += sizeof c;
+    counters_.kernel_launches += d.steps;
+    I.builders_ready = false;
+    if (c[2] != 0) { throw std::length_error("phonon buffer overflow: the device ran out of memory for the population"); }
+}
+
+void Engine::reset() {
+    Impl& I = *impl_;
+    check(cudaMemset(I.tally.p, 0, I.tally.bytes), "memset tally");
+    counters_ = RunCounters{};
+    I.builders_ready = false;
+    I.total = 0;
+}
+
+namespace {
+void unpack(const Engine& eng, Buf& e, Buf& f, cudaStream_t stream, const void* tally) {
+    const SimDesc& d = eng.desc();
+    const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
+    if (e.bytes < SK * sizeof(long long) || e.p == nullptr) { e.alloc(SK * sizeof(long long)); }
+    if (f.bytes < SK * 2 * sizeof(double) || f.p == nullptr) { f.alloc(SK * 2 * sizeof(double)); }
+    if (SK > 0) {
+        const int blocks = static_cast<int>(std::min<std::uint64_t>((SK + 255) / 256, 8192));
+        unpack_kernel<<<blocks, 256, 0, stream>>>(static_cast<const TallySlot*>(tally), d.n_sensors, d.recorded,
+                                                 e.as<long long>(), f.as<double>());
+        check(cudaGetLastError(), "unpack kernel");
+    }
+}
+}// namespace
+
+void Engine::tallies(std::int64_t* energy, double* flux) const {
+    Impl& I = *impl_;
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
+    const std::uint64_t SK = static_cast<std::uint64_t>(desc_.n_sensors) * desc_.recorded;
+    if (energy != nullptr) {
+        check(cudaMemcpyAsync(energy, I.unpacked_energy.p, SK * sizeof(long long), cudaMemcpyDeviceToHost, I.own), "copy energy");
+        counters_.d2h_bytes += SK * sizeof(long long);
+    }
+    if (flux != nullptr) {
+        check(cudaMemcpyAsync(flux, I.unpacked_flux.p, SK * 2 * sizeof(double), cudaMemcpyDeviceToHost, I.own), "copy flux");
+        counters_.d2h_bytes += SK * 2 * sizeof(double);
+    }
+    check(cudaStreamSynchronize(I.own), "tallies sync");
+}
+
+void Engine::interpret(const InterpDesc& d, double* temps, double* fluxes, double* stats) const {
+    Impl& I = *impl_;
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
+    interpret_device(d, I.unpacked_energy.as<long long>(), I.unpacked_flux.as<double>(), temps, fluxes, stats, I.own);
+    const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
+    counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
+                           + d.material.size() * 4 + d.mat_temp_begin.size() * 8;
+    counters_.d2h_bytes += (temps != nullptr ? SK * 8 : 0) + (fluxes != nullptr ? SK * 16 : 0) + (stats != nullptr ? d.n_sensors * 48ULL : 0);
+}
+
+void Engine::final_temps(const InterpDesc& d, std::uint64_t start, double* out) const {
+    Impl& I = *impl_;
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
+    final_temps_device(d, I.unpacked_energy.as<long long>(), start, out, I.own);
+    counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
+                           + d.material.size() * 4 + d.mat_temp_begin.size() * 8;
+    counters_.d2h_bytes += d.n_sensors * 8ULL;
+}
+
+}// namespace psim::gpu

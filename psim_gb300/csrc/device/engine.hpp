@@ -1,0 +1,126 @@
+// Host-side interface of the GPU engine (implemented in engine.cu).  No CUDA types
+// appear here so plain C++ translation units can use it.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace psim::gpu {
+
+constexpr std::uint32_t kMaxMaterialsHost = 16;
+
+// Owning copy of psim_sim_desc (include/psim_gb300.h).
+struct SimDesc {
+    std::uint64_t steps{ 0 };
+    double sim_time{ 0. };
+    bool phasor{ false };
+    int sim_type{ 0 };
+    std::uint64_t step_adj{ 0 };
+    std::uint64_t recorded{ 0 };
+    bool full{ false };
+    std::uint32_t n_materials{ 0 };
+    std::vector<double> mat_freq;   // [M][1000]
+    std::vector<double> mat_vel;    // [M][2][1000]
+    std::vector<double> mat_params; // [M][8]
+    std::uint32_t n_tables{ 0 };
+    std::vector<double> tables;     // [T][1000][2]
+    std::uint32_t n_sensors{ 0 };
+    std::vector<std::uint32_t> sensor_material, sensor_base_table, sensor_scatter_table;
+    std::vector<double> sensor_temp;
+    std::uint32_t n_cells{ 0 };
+    std::vector<double> cell_vertices;// [C][6]
+    std::vector<std::uint32_t> cell_sensor;
+    std::vector<double> cell_spec;
+    std::vector<std::uint32_t> edge_sub_begin;// [3C+1]
+    std::vector<std::int32_t> sub_kind;
+    std::vector<std::uint32_t> sub_target;
+    std::vector<double> sub_line;// [n_subs][4]
+    std::uint32_t n_emitters{ 0 };
+    std::vector<std::uint32_t> emit_cell, emit_edge, emit_table;
+    std::vector<double> emit_line, emit_temp, emit_start, emit_duration;
+};
+
+struct RunCounters {
+    std::uint64_t phonons{ 0 };
+    std::uint64_t phonon_steps{ 0 };
+    std::uint64_t kernel_launches{ 0 };
+    std::uint64_t relocations{ 0 };
+    std::uint64_t overflow{ 0 };
+    std::uint64_t max_population{ 0 };
+    std::uint64_t event_limits{ 0 };
+    std::uint64_t h2d_bytes{ 0 };
+    std::uint64_t d2h_bytes{ 0 };
+    double kernel_ms{ 0. };
+};
+
+// Interpreter inputs (SensorInterpreter state plus the per-sensor quantities it reads).
+struct InterpDesc {
+    std::uint32_t n_sensors{ 0 };
+    std::uint64_t recorded{ 0 };
+    double t_eq{ 0. };
+    double eff_energy{ 0. };
+    double lb{ 0. }, ub{ 0. };
+    std::vector<double> area, heat_capacity, init_temp;
+    std::vector<std::uint32_t> material;
+    std::vector<std::uint64_t> mat_temp_begin;// [M+1]
+    std::vector<double> temps, energies;
+};
+
+class Engine {
+public:
+    explicit Engine(const SimDesc& desc);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    // Phonon counts per cell and emitter (initPhononBuilders) and the birth schedule.
+    std::uint64_t init_builders(double t_eq, double eff_energy, const double* cell_energy, const double* emit_energy,
+                                const double* sensor_init_temp, std::uint64_t seed);
+    // Every measurement step; stream may be null (the engine's own stream).
+    void run(int precision, void* stream);
+    void reset();
+    void set_step_adjustment(std::uint64_t adj) { desc_.step_adj = adj; }
+    void set_use_graph(bool on) { use_graph_ = on; }
+    void set_grid(int blocks) { grid_override_ = blocks; }
+
+    // Raw tallies (host): energy[S][K], flux[S][K][2].
+    void tallies(std::int64_t* energy, double* flux) const;
+    // Device-resident interpretation of the current tallies.
+    void interpret(const InterpDesc& d, double* temps, double* fluxes, double* stats) const;
+    void final_temps(const InterpDesc& d, std::uint64_t start, double* out) const;
+
+    const RunCounters& counters() const noexcept { return counters_; }
+    // bytes copied host->device when the model was created (geometry, tables, materials)
+    std::uint64_t model_bytes() const noexcept { return model_bytes_; }
+    void add_h2d(std::uint64_t bytes) const noexcept { counters_.h2d_bytes += bytes; }
+    const SimDesc& desc() const noexcept { return desc_; }
+    void* stream() const noexcept { return stream_; }
+
+private:
+    struct Impl;
+    SimDesc desc_;
+    std::unique_ptr<Impl> impl_;
+    void* stream_{ nullptr };
+    mutable RunCounters counters_;
+    std::uint64_t model_bytes_{ 0 };
+    bool use_graph_{ true };
+    int grid_override_{ 0 };
+};
+
+// Stand-alone interpreter on host arrays (psim_interpret / psim_final_temps).
+void interpret_host(const InterpDesc& d, const std::int64_t* energy, const double* flux, double* temps, double* fluxes,
+                    double* stats);
+void final_temps_host(const InterpDesc& d, const std::int64_t* energy, std::uint64_t start, double* out);
+
+// FP64 geometry kernels (bit-exact with the reference routines).
+void geom_intersect(std::int64_t n, const double* a, const double* b, double* poi, std::int32_t* has);
+void geom_on_line(std::int64_t n, const double* lines, const double* pts, std::int32_t* out);
+void geom_tri_contains(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
+void geom_edge_index(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
+
+int device_count() noexcept;
+
+}// namespace psim::gpu

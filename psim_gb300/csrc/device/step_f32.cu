@@ -1,0 +1,359 @@
+// FP32 cell-local phonon transport: one launch advances every phonon across one
+// measurement step (ModelSimulator::simulatePhonon, psim/src/modelSimulator.cpp:139-198,
+// reorganised step by step instead of phonon by phonon).
+//
+// Per phonon and step: load 32 B of state (or create the phonon if it is born in this
+// step), run events until the step boundary or absorption, tally at the boundary, and
+// write the 32 B survivor record to the compacted output buffer.
+//
+// Geometry: positions are relative to the cell's first vertex.  The exit time through
+// edge e is (h_e - n_e.p) / (n_e.w) for edges the phonon moves towards (n_e.w > 0), the
+// edge it entered through excluded; for a triangle this is the first boundary the
+// straight path meets, the impact the reference finds with Line::getIntersection
+// (psim/src/modelSimulator.cpp:87-122).  What happens at the impact follows the
+// reference: Cell::handleSurfaceCollision -> CompositeSurface::handlePhonon
+// (psim/src/cell.cpp:103-108, psim/src/compositeSurface.cpp:47-66) resolves each edge
+// to its first transition surface, else its first emitting surface, else the boundary.
+#include "transport.cuh"
+
+namespace psim::gpu {
+namespace {
+
+struct Ph32 {
+    float px, py, dx, dy;
+    std::uint32_t meta, binw;
+    float tts;
+    std::uint32_t id;
+};
+
+// Group velocity of the phonon's bin (Material::getVel, psim/src/material.cpp:82-84).
+__device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
+    return phasor ? 1000.f
+                  : __ldg(P.vel32 + (smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw));
+}
+
+// Frequency in units of 1e13 rad/s (Material::getFreq, psim/src/material.cpp:77-80): bin
+// centre plus the stored uniform offset inside the bin in a deviational simulation.
+__device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
+    if (phasor) { return 1e-13f; }
+    const std::uint32_t sm = smat_of(binw);
+    const float c = __ldg(P.centre32 + sm * kBins + bin_of(binw));
+    if (P.full_sim) { return c; }
+    const float u = (static_cast<float>(jitter_of(binw)) + 0.5f) * (1.0f / 262144.0f);
+    return c + (2.f * u - 1.f) * (P.materials[sm].width * 0.5f);
+}
+
+// Relaxation rates [N, U, I] (Material::tauNInv/tauUInv/tauIInv, psim/src/material.cpp:207-239),
+// frequency w in 1e13 rad/s, coefficients pre-scaled so every factor stays in FP32 range.
+__device__ __forceinline__ float3 rates32(const MaterialDev& m, const SensorDev& s, float w, int pol) {
+    const float w2 = w * w;
+    float n;
+    float u;
+    if (pol == 0) {
+        n = m.cL * w2 * s.T3;
+        u = n;
+    } else {
+        n = (w < m.w_cut) ? m.cTN * w * s.T4 : 0.f;
+        u = (w >= m.w_cut) ? m.cTU * w2 / sinhf(w * s.xk) : 0.f;
+    }
+    return make_float3(n, u, m.cI * w2 * w2);
+}
+
+// Phonon::setRandDirection (psim/src/phonon.cpp:28-31): dx = 2u-1, dy = sqrt(1-dx^2) cos(2 pi u').
+__device__ __forceinline__ void iso_dir(Ph32& p, Stream& rs) {
+    const float dx = 2.f * rs.uf() - 1.f;
+    p.dx = dx;
+    p.dy = sqrtf(fmaxf(0.f, 1.f - dx * dx)) * __cosf(6.2831853071795865f * rs.uf());
+}
+
+// Surface::redirectPhonon (psim/src/surface.cpp:23-30): Lambertian about the inward normal n.
+__device__ __forceinline__ void diffuse_dir(Ph32& p, Stream& rs, float nx, float ny) {
+    const float u = rs.uf();
+    const float a = sqrtf(u);
+    const float b = sqrtf(1.f - u) * __cosf(6.2831853071795865f * rs.uf());
+    p.dx = nx * a - ny * b;
+    p.dy = ny * a + nx * b;
+}
+
+// Surface::boundaryHandlePhonon (psim/src/surface.cpp:32-44): specular with probability spec.
+__device__ __forceinline__ void reflect(Ph32& p, Stream& rs, float spec, float4 e) {
+    if (spec >= 1.f || (spec > 0.f && rs.uf() < spec)) {
+        const float dn = p.dx * e.x + p.dy * e.y;
+        p.dx -= 2.f * dn * e.x;
+        p.dy -= 2.f * dn * e.y;
+    } else {
+        diffuse_dir(p, rs, -e.x, -e.y);
+    }
+}
+
+// Material::freqIndex + getFreq (psim/src/material.cpp:64-80) from an alias table of the
+// material 'mat'.
+__device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
+                                            std::uint32_t mat) {
+    const std::uint32_t o = alias_draw(P.alias + static_cast<std::size_t>(table) * kAliasCols, rs.next());
+    const std::uint32_t jit = P.full_sim ? 0U : (rs.next() >> 14);
+    p.binw = make_binw(o >> 1, mat, jit);
+    p.meta = meta_with_pol(p.meta, static_cast<int>(o & 1U));
+}
+
+// Create newborn j of this step (CellOriginBuilder / SurfaceOriginBuilder / PhasorBuilder,
+// psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
+__device__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
+    const BirthGroup g = P.groups[find_group(P, j)];
+    p.id = P.id_base + j;
+    rs.init(P.key0, P.key1, P.step, p.id);
+    p.tts = 0.f;
+    if (g.source >= 0) {
+        const std::uint32_t cell = static_cast<std::uint32_t>(g.source);
+        const CellF32& c = P.cells32[cell];
+        p.meta = make_meta(cell, kNoEdge, 0, g.sign, false);
+        sample_freq(P, p, rs, P.sensors[c.sensor].base_table, c.material);
+        float r1 = rs.uf();
+        float r2 = rs.uf();
+        if (r1 + r2 > 1.f) {
+            r1 = 1.f - r1;
+            r2 = 1.f - r2;
+        }
+        p.px = c.vert[1].x * r1 + c.vert[2].x * r2;
+        p.py = c.vert[1].y * r1 + c.vert[2].y * r2;
+        iso_dir(p, rs);
+        return P.dt;
+    }
+    const EmitterDev& e = P.emitters[static_cast<std::uint32_t>(-(g.source + 1))];
+    const float t_birth = g.t0 + g.span * rs.uf();
+    const bool phasor = P.phasor_sim != 0;
+    p.meta = make_meta(e.cell, e.edge, 0, g.sign, phasor);
+    sample_freq(P, p, rs, e.table, P.cells32[e.cell].material);
+    const float r = rs.uf();
+    p.px = e.a.x * r + e.b.x * (1.f - r);
+    p.py = e.a.y * r + e.b.y * (1.f - r);
+    if (phasor) {
+        p.binw = make_binw(1U, smat_of(p.binw), 0U);
+        p.meta = meta_with_pol(p.meta, 0);
+        p.dx = e.nx;
+        p.dy = e.ny;
+    } else {
+        diffuse_dir(p, rs, e.nx, e.ny);
+    }
+    return fmaxf(P.dt - t_birth, 0.f);
+}
+
+struct Outcome {
+    bool alive;
+    bool boundary;// reached the step boundary (a phonon-step), alive or at the last boundary
+    bool tallied;
+    std::uint32_t sensor;
+    long long fx, fy;
+};
+
+// Events of one phonon until the step boundary (or absorption).
+__device__ Outcome transport32(const StepParams& P, Ph32& p, Stream& rs, float rem, unsigned long long& relocations,
+                               unsigned long long& limits) {
+    Outcome out{ false, false, false, 0U, 0, 0 };
+    std::uint32_t cell = meta_cell(p.meta);
+    const CellF32* C = P.cells32 + cell;
+    std::uint32_t sensor = C->sensor;
+    std::uint32_t mat = C->material;
+    const bool phasor = meta_phasor(p.meta);
+    int pol = meta_pol(p.meta);
+    float v = vel32(P, p.binw, pol, phasor);
+    unsigned events = 0;
+    while (true) {
+        if (++events > kMaxEventsPerStep) {// numerical corner case: end the step where the phonon is
+            ++limits;
+            rem = 0.f;
+            p.tts = fmaxf(p.tts, 0.f);
+        }
+        if (p.tts <= 0.f) {// draw the time to the next scattering event (modelSimulator.cpp:148-153)
+            const float3 r = rates32(P.materials[mat], P.sensors[sensor], omega32(P, p.binw, phasor), pol);
+            p.tts = 1e9f * (-__logf(rs.uf())) / (r.x + r.y + r.z);
+        }
+        const bool meas = rem <= p.tts;
+        const float target = meas ? rem : p.tts;
+        float drifted = 0.f;
+        int ncoll = 0;
+        bool changed = false;
+        while (true) {// handleImpacts / nextImpact (modelSimulator.cpp:87-122, 205-225)
+            const float wx = p.dx * v;
+            const float wy = p.dy * v;
+            const std::uint32_t entry = meta_edge(p.meta);
+            float tbest = 3.0e38f;
+            int ebest = -1;
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                const float4 E = C->edge[e];
+                const float den = E.x * wx + E.y * wy;
+                if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
+                    const float t = fmaxf((E.z - (E.x * p.px + E.y * p.py)) / den, 0.f);
+                    if (t < tbest) {
+                        tbest = t;
+                        ebest = e;
+                    }
+                }
+            }
+            const float left = target - drifted;
+            if (ebest < 0 || tbest > left) {
+                p.px += wx * left;
+                p.py += wy * left;
+                drifted = target;
+                break;
+            }
+            p.px += wx * tbest;
+            p.py += wy * tbest;
+            drifted += tbest;
+            const float4 E = C->edge[ebest];
+            const int link = C->link[ebest];
+            std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
+            if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
+                const CellF32* N = P.cells32 + link;
+                bool pass = true;
+                if (N->material != mat) {
+                    const MaterialDev& mt = P.materials[N->material];
+                    const float w = omega32(P, p.binw, phasor);
+                    pass = !(w > (pol == 0 ? mt.w_max_la : mt.w_max_ta));
+                }
+                if (pass) {
+                    p.px += C->offset[ebest].x;
+                    p.py += C->offset[ebest].y;
+                    entry_next = (C->rev >> (2 * ebest)) & 3U;
+                    cell = static_cast<std::uint32_t>(link);
+                    C = N;
+                    if (C->sensor != sensor) {
+                        sensor = C->sensor;
+                        changed = true;
+                    }
+                    mat = C->material;
+                } else {
+                    const float flip = ((C->rev >> (8 + ebest)) & 1U) ? -1.f : 1.f;
+                    diffuse_dir(p, rs, -E.x * flip, -E.y * flip);
+                }
+            } else if (link == -1) {
+                reflect(p, rs, C->spec, E);
+            } else {// EmitSurface::handlePhonon (psim/src/surface.cpp:61-65)
+                const EmitterDev& em = P.emitters[static_cast<std::uint32_t>(-(link + 2))];
+                if (P.step >= em.absorb_lo && P.step <= em.absorb_hi) { return out; }// absorbed
+                reflect(p, rs, C->spec, E);
+            }
+            p.meta = meta_with_cell_edge(p.meta, cell, entry_next);
+            if (++ncoll > kMaxCollisions) {// stuck in a corner: random point in the cell
+                float r1 = rs.uf();
+                float r2 = rs.uf();
+                if (r1 + r2 > 1.f) {
+                    r1 = 1.f - r1;
+                    r2 = 1.f - r2;
+                }
+                p.px = C->vert[1].x * r1 + C->vert[2].x * r2;
+                p.py = C->vert[1].y * r1 + C->vert[2].y * r2;
+                p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
+                drifted = target;
+                ++relocations;
+                break;
+            }
+            if (changed) { break; }
+        }
+        const float used = changed ? drifted : target;
+        rem -= used;
+        p.tts -= used;
+        if (rem == 0.f) {// measurement boundary (modelSimulator.cpp:182-188)
+            const std::uint32_t next = P.step + 1U;
+            out.boundary = true;
+            if (next >= P.n_steps) { return out; }
+            out.alive = true;
+            if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
+                const int sign = meta_sign(p.meta);
+                out.tallied = true;
+                out.sensor = sensor;
+                out.fx = __float2ll_rn(static_cast<float>(sign) * v * p.dx * kFluxScale);
+                out.fy = __float2ll_rn(static_cast<float>(sign) * v * p.dy * kFluxScale);
+            }
+            return out;
+        }
+        if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
+            const float3 r = rates32(P.materials[mat], P.sensors[sensor], omega32(P, p.binw, phasor), pol);
+            const float sum = r.x + r.y + r.z;
+            const float u = rs.uf();
+            if (u <= (r.x + r.y) / sum) {
+                sample_freq(P, p, rs, P.sensors[sensor].scatter_table, mat);
+                pol = meta_pol(p.meta);
+                v = vel32(P, p.binw, pol, phasor);
+                if (u > r.x / sum) {
+                    iso_dir(p, rs);
+                    p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
+                }
+            } else if (r.z > 0.f) {
+                iso_dir(p, rs);
+                p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
+            }
+        } else {
+            p.tts = 0.f;// new sensor area (or phasor): draw a fresh scattering time
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) step_kernel_f32(const StepParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    BlockTally bt;
+    tally_init(P, bt, smem);
+    const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *P.count_clear = 0U;
+        atomicMax(P.counters + 3, static_cast<unsigned long long>(n_alive) + P.n_new);
+    }
+    const std::uint32_t total = n_alive + P.n_new;
+    const std::uint32_t slot_k = P.step + 1U >= P.step_adj ? P.step + 1U - P.step_adj : 0U;
+    const float4* in_pd = static_cast<const float4*>(P.in);
+    const uint4* in_meta = reinterpret_cast<const uint4*>(in_pd + P.capacity);
+    float4* out_pd = static_cast<float4*>(P.out);
+    uint4* out_meta = reinterpret_cast<uint4*>(out_pd + P.capacity);
+    unsigned long long steps = 0;
+    unsigned long long relocations = 0;
+    unsigned long long limits = 0;
+    const std::uint32_t stride = gridDim.x * blockDim.x;
+    for (std::uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
+        const std::uint32_t i = base + threadIdx.x;
+        Outcome o{ false, false, false, 0U, 0, 0 };
+        Ph32 p{ 0.f, 0.f, 0.f, 0.f, 0U, 0U, 0.f, 0U };
+        if (i < total) {
+            Stream rs;
+            float rem;
+            if (i < n_alive) {
+                const float4 a = in_pd[i];
+                const uint4 b = in_meta[i];
+                p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
+                rs.init(P.key0, P.key1, P.step, p.id);
+                rem = P.dt;
+            } else {
+                rem = spawn32(P, p, rs, i - n_alive);
+            }
+            o = transport32(P, p, rs, rem, relocations, limits);
+            steps += o.boundary ? 1ULL : 0ULL;
+        }
+        const std::uint32_t slot = reserve_slot(P, o.alive);
+        if (slot != 0xFFFFFFFFU) {
+            out_pd[slot] = make_float4(p.px, p.py, p.dx, p.dy);
+            out_meta[slot] = make_uint4(p.meta, p.binw, __float_as_uint(p.tts), p.id);
+        }
+        tally_add(P, bt, o.tallied, o.sensor, meta_sign(p.meta), o.fx, o.fy, slot_k);
+    }
+    block_count_add(P.counters + 0, steps);
+    block_count_add(P.counters + 1, relocations);
+    block_count_add(P.counters + 4, limits);
+    tally_flush(P, bt, slot_k);
+}
+
+}// namespace
+
+void launch_step_f32(const StepParams& P, int grid, cudaStream_t stream) {
+    step_kernel_f32<<<grid, kBlock, kTallySmem, stream>>>(P);
+}
+
+int occupancy_f32() {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f32, kBlock, kTallySmem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return blocks;
+}
+
+}// namespace psim::gpu

@@ -1,0 +1,123 @@
+// Pieces shared by the FP32 and FP64 transport kernels: alias sampling, births,
+// warp-aggregated tallies and stream compaction.
+#pragma once
+
+#include "common.cuh"
+
+namespace psim::gpu {
+
+constexpr int kBlock = 256;
+constexpr int kSharedSensors = 2048;   // sensors tallied in shared memory; larger models use global atomics
+
+// Walker alias table over the 2000 (bin, polarization) outcomes, one 32-bit word per column:
+// a 21-bit acceptance threshold and an 11-bit alias column.  One 32-bit random word picks the
+// column (top 11 bits) and decides acceptance (low 21 bits).
+__device__ __forceinline__ std::uint32_t alias_draw(const std::uint32_t* table, std::uint32_t x) {
+    const std::uint32_t col = x >> 21;
+    const std::uint32_t e = __ldg(table + col);
+    const std::uint32_t o = ((x & 0x1FFFFFU) < (e >> 11)) ? col : (e & 0x7FFU);
+    return min(o, static_cast<std::uint32_t>(2 * kBins - 1));// columns >= 2000 carry no probability
+}
+
+// Newborn j of this step -> its birth group (groups sorted by 'first').
+__device__ __forceinline__ std::uint32_t find_group(const StepParams& P, std::uint32_t j) {
+    std::uint32_t lo = P.group_begin;
+    std::uint32_t hi = P.group_end;// groups[lo].first <= j < groups[hi].first (hi exclusive)
+    while (hi - lo > 1) {
+        const std::uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&P.groups[mid].first) <= j) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
+}
+
+// Shared-memory tally of one block for the boundary this step ends on.
+struct BlockTally {
+    int* count;
+    long long* fx;
+    long long* fy;
+    bool shared;
+};
+
+__device__ __forceinline__ void tally_add(const StepParams& P, BlockTally& bt, bool tallied, std::uint32_t sensor,
+                                          int sign, long long fx, long long fy, std::uint32_t slot) {
+    const unsigned full = 0xFFFFFFFFU;
+    const int key = tallied ? static_cast<int>(sensor) : -1;
+    const unsigned peers = __match_any_sync(full, key);
+    if (key < 0) { return; }
+    const int lane = static_cast<int>(threadIdx.x & 31U);
+    const int leader = __ffs(static_cast<int>(peers)) - 1;
+    const int c = __reduce_add_sync(peers, sign);
+    if (bt.shared) {
+        if (lane == leader) { atomicAdd(bt.count + sensor, c); }
+        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx + sensor), static_cast<unsigned long long>(fx));
+        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy + sensor), static_cast<unsigned long long>(fy));
+    } else {
+        TallySlot* t = P.tally + static_cast<std::size_t>(slot) * P.n_sensors + sensor;
+        if (lane == leader) { atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(c))); }
+        atomicAdd(reinterpret_cast<unsigned long long*>(&t->fx), static_cast<unsigned long long>(fx));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&t->fy), static_cast<unsigned long long>(fy));
+    }
+}
+
+__device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt, std::uint32_t slot) {
+    if (!bt.shared) { return; }
+    __syncthreads();
+    for (std::uint32_t s = threadIdx.x; s < P.n_sensors; s += blockDim.x) {
+        const int c = bt.count[s];
+        const long long fx = bt.fx[s];
+        const long long fy = bt.fy[s];
+        if (c != 0 || fx != 0 || fy != 0) {
+            TallySlot* t = P.tally + static_cast<std::size_t>(slot) * P.n_sensors + s;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(c)));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fx), static_cast<unsigned long long>(fx));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fy), static_cast<unsigned long long>(fy));
+        }
+    }
+}
+
+__device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, unsigned char* smem) {
+    bt.shared = P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors);
+    bt.fx = reinterpret_cast<long long*>(smem);
+    bt.fy = bt.fx + kSharedSensors;
+    bt.count = reinterpret_cast<int*>(bt.fy + kSharedSensors);
+    if (bt.shared) {
+        for (std::uint32_t s = threadIdx.x; s < P.n_sensors; s += blockDim.x) {
+            bt.fx[s] = 0;
+            bt.fy[s] = 0;
+            bt.count[s] = 0;
+        }
+    }
+    __syncthreads();
+}
+
+constexpr std::size_t kTallySmem = kSharedSensors * (2 * sizeof(long long) + sizeof(int));
+
+// Warp-aggregated slot reservation in the output buffer; returns the slot or UINT32_MAX.
+__device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool alive) {
+    const unsigned full = 0xFFFFFFFFU;
+    const unsigned mask = __ballot_sync(full, alive);
+    const int lane = static_cast<int>(threadIdx.x & 31U);
+    std::uint32_t base = 0;
+    if (lane == 0 && mask != 0U) { base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(mask))); }
+    base = __shfl_sync(full, base, 0);
+    if (!alive) { return 0xFFFFFFFFU; }
+    const std::uint32_t slot = base + static_cast<std::uint32_t>(__popc(mask & ((1U << lane) - 1U)));
+    if (slot >= P.capacity) {
+        atomicAdd(P.counters + 2, 1ULL);
+        return 0xFFFFFFFFU;
+    }
+    return slot;
+}
+
+__device__ __forceinline__ void block_count_add(unsigned long long* target, unsigned long long v) {
+    const unsigned full = 0xFFFFFFFFU;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { v += __shfl_down_sync(full, v, o); }
+    if ((threadIdx.x & 31U) == 0U && v != 0ULL) { atomicAdd(target, v); }
+}
+
+}// namespace psim::gpu

@@ -1,0 +1,36 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA device (GB300)")
+    config.addinivalue_line("markers", "slow: longer statistical runs")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Builds libpsim_gb300.so and the CPU oracle once per session."""
+    from psim_gb300 import build
+    from oracle import oracle
+    build.build()
+    oracle.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def gpu(built):
+    from psim_gb300 import api
+    if api.device_count() < 1:
+        pytest.fail("no CUDA device visible to libpsim_gb300 (GPU tests need a GB300)")
+    return True
+
+
+def model_path(name: str) -> str:
+    return os.path.join(GOLDEN, "models", name + ".json")

@@ -1,0 +1,272 @@
+"""Generates the golden fixtures in tests/golden/ from the reference psim built from its own
+sources (oracle/_ref/ref_driver, see oracle/ref_recipe/Makefile).  Run it where the
+reference tree is available:
+
+    python tests/golden/make_golden.py [--reference /path/to/reference] [--skip-runs]
+
+Outputs (all small):
+  models/*.json          the model files the fixtures were made from (psim_gb300.modelgen)
+  geom.npz               Line::getIntersection / Line::contains(Point) / Triangle::contains /
+                         Triangle normals, area and getRandPoint on random and degenerate cases
+  tables_<model>.npz     material tables after Model::initializeMaterialTables
+  invert_<model>.npz     SensorInterpreter results for given tallies
+  runs_<model>.npz       per-sensor results of 16 seeded reference runs (statistical parity)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from psim_gb300 import modelgen as mg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.golden.tables_io import read_tables  # noqa: E402
+
+MODELS = os.path.join(HERE, "models")
+SEEDS = list(range(1, 17))
+
+
+def model_specs():
+    """Small models of the benchmark shapes (same geometry family, reduced sizes)."""
+    return {
+        "bar_ss": mg.bar(num_phonons=100000, num_measurements=1000, sim_time=5.0),
+        "bar_full": mg.bar(num_phonons=50000, num_measurements=1000, sim_time=5.0, t_eq=0.0, t_left=60.0,
+                           t_right=40.0, t_init=50.0),
+        "bar_periodic": mg.bar(num_phonons=50000, num_measurements=500, sim_time=2.5, sim_type=1, step_interval=25,
+                               spec=0.3),
+        "kinked_small": mg.kinked(num_phonons=60000, num_measurements=400, sim_time=2.0, n_len=10, step_interval=20),
+        "plate_small": mg.plate(length=1000.0, width=250.0, nx=16, ny=4, strip=(100.0, 150.0), num_phonons=60000,
+                                num_measurements=400, sim_time=0.4, pulse=0.02, step_interval=20),
+        "bar_runs": mg.bar(num_phonons=30000, num_measurements=400, sim_time=2.0, num_runs=3, spec=0.5),
+        "bar_phasor": mg.bar(num_phonons=20000, num_measurements=400, sim_time=2.0, sim_type=1, step_interval=20,
+                             phasor_sim=True),
+    }
+
+
+def write_models():
+    os.makedirs(MODELS, exist_ok=True)
+    paths = {}
+    for name, m in model_specs().items():
+        p = os.path.join(MODELS, name + ".json")
+        mg.write(m, p)
+        paths[name] = p
+    return paths
+
+
+def driver(*args, env=None):
+    out = subprocess.run([O.REF_DRIVER, *args], capture_output=True, text=True, env=env)
+    if out.returncode != 0:
+        raise RuntimeError(f"ref_driver {args} failed: {out.stderr}")
+    return out.stdout
+
+
+# ---------------------------------------------------------------- geometry
+def geometry_cases(rng: np.random.Generator):
+    lines = []
+    # random segments, half on a coarse grid to create collinear/parallel/touching cases
+    for i in range(4000):
+        if i % 2:
+            a = rng.integers(-3, 4, size=4).astype(float) * 25.0
+            b = rng.integers(-3, 4, size=4).astype(float) * 25.0
+        else:
+            a = rng.uniform(-100, 100, size=4)
+            b = rng.uniform(-100, 100, size=4)
+        if i % 7 == 0:
+            b[2] = b[0]  # vertical
+        if i % 11 == 0:
+            a[3] = a[1]  # horizontal
+        if i % 13 == 0:
+            b[:2] = a[2:]  # touching at an end point
+        if i % 17 == 0:
+            a[2:] = a[:2]  # degenerate (identical end points)
+        lines.append("I " + " ".join(repr(float(v)) for v in np.concatenate([a, b])))
+    intersect = [list(map(float, l.split()[1:])) for l in lines]
+    # point on line: points on, near and off random lines (including the end points)
+    on = []
+    for i in range(3000):
+        l = rng.uniform(-50, 50, size=4)
+        if i % 5 == 0:
+            l[2] = l[0]
+        t = rng.uniform(-0.5, 1.5)
+        p = l[:2] + t * (l[2:] - l[:2])
+        if i % 3 == 1:
+            p = p + rng.normal(scale=1e-9, size=2)
+        elif i % 3 == 2:
+            p = p + rng.normal(scale=1.0, size=2)
+        on.append(np.concatenate([l, p]))
+    # triangles: random and grid-snapped, points inside/outside/on edges/at vertices
+    tri = []
+    for i in range(3000):
+        t = rng.uniform(-50, 50, size=6) if i % 2 else rng.integers(-2, 3, size=6).astype(float) * 10.0
+        w = rng.dirichlet([1, 1, 1])
+        if i % 4 == 1:
+            w[rng.integers(0, 3)] = 0.0
+            w = w / w.sum()
+        p = w[0] * t[0:2] + w[1] * t[2:4] + w[2] * t[4:6]
+        if i % 4 == 2:
+            p = p + rng.normal(scale=5.0, size=2)
+        if i % 4 == 3:
+            p = t[2 * (i % 3): 2 * (i % 3) + 2].copy()
+        tri.append(np.concatenate([t, p]))
+    rand_pts = []
+    for i in range(500):
+        t = rng.uniform(-50, 50, size=6)
+        r = rng.uniform(0, 1, size=2)
+        rand_pts.append(np.concatenate([t, r]))
+    return np.array(intersect), np.array(on), np.array(tri), np.array(rand_pts)
+
+
+def make_geom():
+    rng = np.random.default_rng(20261203)
+    inter, on, tri, rnd = geometry_cases(rng)
+    with tempfile.TemporaryDirectory() as td:
+        cases = os.path.join(td, "cases.txt")
+        out = os.path.join(td, "out.txt")
+        with open(cases, "w") as f:
+            for r in inter:
+                f.write("I " + " ".join(repr(float(v)) for v in r) + "\n")
+            for r in on:
+                f.write("L " + " ".join(repr(float(v)) for v in r) + "\n")
+            for r in tri:
+                f.write("C " + " ".join(repr(float(v)) for v in r) + "\n")
+            for r in tri:
+                f.write("N " + " ".join(repr(float(v)) for v in r[:6]) + "\n")
+            for r in rnd:
+                f.write("R " + " ".join(repr(float(v)) for v in r) + "\n")
+        driver("geom", cases, out)
+        rows = open(out).read().splitlines()
+    k = 0
+    has = np.zeros(len(inter), dtype=np.int32)
+    poi = np.zeros((len(inter), 2))
+    for i in range(len(inter)):
+        parts = rows[k].split()
+        k += 1
+        if parts[0] == "X":
+            has[i] = -1
+        elif parts[0] == "1":
+            has[i] = 1
+            poi[i] = [float(parts[1]), float(parts[2])]
+    on_out = np.array([int(rows[k + i]) if rows[k + i] != "X" else -1 for i in range(len(on))], dtype=np.int32)
+    k += len(on)
+    tri_out = np.array([int(rows[k + i]) if rows[k + i] not in ("X", "E") else -2 for i in range(len(tri))], dtype=np.int32)
+    k += len(tri)
+    normals = np.full((len(tri), 8), np.nan)
+    for i in range(len(tri)):
+        parts = rows[k + i].split()
+        if parts[0] != "X":
+            normals[i] = [float(v) for v in parts]
+    k += len(tri)
+    rnd_out = np.array([[float(v) for v in rows[k + i].split()] for i in range(len(rnd))])
+    np.savez_compressed(os.path.join(HERE, "geom.npz"), intersect_a=inter[:, :4], intersect_b=inter[:, 4:],
+                        intersect_has=has, intersect_poi=poi, online_lines=on[:, :4], online_pts=on[:, 4:],
+                        online_out=on_out, tri=tri[:, :6], tri_pts=tri[:, 6:], tri_out=tri_out, tri_normals=normals,
+                        rand_tri=rnd[:, :6], rand_r=rnd[:, 6:], rand_out=rnd_out)
+    print("geom.npz:", len(inter), "intersections,", int((has == 1).sum()), "hits")
+
+
+# ---------------------------------------------------------------- tables
+def make_tables(paths):
+    for name in ("bar_ss", "bar_full", "kinked_small"):
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "t.bin")
+            driver("tables", paths[name], out)
+            mats, bounds = read_tables(out)
+        m = mats[0]
+        nt = len(m["temps"])
+        keep = sorted(set([0, nt // 2, nt - 1] + [int(np.searchsorted(m["temps"], t)) for t in (300.0, 310.0, 290.0, 50.0, 60.0, 40.0, 320.0, 280.0) if m["temps"][0] <= t <= m["temps"][-1]]))
+        np.savez_compressed(os.path.join(HERE, f"tables_{name}.npz"), temps=m["temps"], freq=m["freq"],
+                            vel_la=m["vel_la"], vel_ta=m["vel_ta"], dens_la=m["dens_la"], dens_ta=m["dens_ta"],
+                            base_sum=m["base_sum"], emit_sum=m["emit_sum"], scatter_sum=m["scatter_sum"],
+                            keep=np.array(keep), base=m["base"][keep], emit=m["emit"][keep], scatter=m["scatter"][keep],
+                            bounds=bounds)
+        print(f"tables_{name}.npz: {nt} temperatures, kept {keep}")
+
+
+# ---------------------------------------------------------------- inversion
+def make_invert(paths):
+    rng = np.random.default_rng(7)
+    for name in ("bar_ss", "bar_full", "kinked_small"):
+        shape = O.shape(paths[name])
+        S, K = shape[0], shape[1]
+        scale = 40 if name != "bar_full" else 4000
+        counts = rng.integers(-scale, scale, size=(S, K))
+        if name == "bar_full":
+            counts = np.abs(counts) + rng.integers(0, 20000, size=(S, K))
+        with tempfile.TemporaryDirectory() as td:
+            cp = os.path.join(td, "c.txt")
+            op = os.path.join(td, "o.txt")
+            with open(cp, "w") as f:
+                for s in range(S):
+                    f.write(f"{s} {K} " + " ".join(str(int(v)) for v in counts[s]) + "\n")
+            driver("invert", paths[name], cp, op)
+            rows = open(op).read().splitlines()
+        eff = float(rows[0].split()[1])
+        stats = np.zeros((S, 6))
+        temps = np.zeros((S, K))
+        for r in rows[1:]:
+            v = r.split()
+            s = int(v[0])
+            stats[s] = [float(x) for x in v[1:7]]
+            temps[s] = [float(x) for x in v[7:]]
+        np.savez_compressed(os.path.join(HERE, f"invert_{name}.npz"), counts=counts, flux_x_factor=1000.5,
+                            flux_y_factor=-250.25, eff=eff, stats=stats, temps=temps)
+        print(f"invert_{name}.npz: eff {eff:.6e}")
+
+
+# ---------------------------------------------------------------- statistical references
+def ref_run(path, seed):
+    with tempfile.TemporaryDirectory() as td:
+        dump = os.path.join(td, "d.json")
+        env = dict(os.environ, PSIM_SEED=str(seed))
+        driver("run", path, dump, env=env)
+        d = json.load(open(dump))
+    runs = [np.array([m["stats"] for m in run]) for run in d["runs"]]
+    acc = np.zeros_like(runs[0])
+    for r in runs:
+        acc = acc + r
+    return acc / len(runs), d["total_phonons_last_run"]
+
+
+def make_runs(paths, names):
+    for name in names:
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+            res = list(pool.map(lambda s: ref_run(paths[name], s), SEEDS))
+        stats = np.stack([r[0] for r in res])
+        phonons = np.array([r[1] for r in res])
+        np.savez_compressed(os.path.join(HERE, f"runs_{name}.npz"), seeds=np.array(SEEDS), stats=stats, phonons=phonons)
+        print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--skip-runs", action="store_true")
+    ap.add_argument("--only", default="")
+    args = ap.parse_args()
+    if not O.build_reference(args.reference):
+        sys.exit("the reference sources are not available")
+    O.build()
+    paths = write_models()
+    only = set(args.only.split(",")) if args.only else None
+    if only is None or "geom" in only:
+        make_geom()
+    if only is None or "tables" in only:
+        make_tables(paths)
+    if only is None or "invert" in only:
+        make_invert(paths)
+    if not args.skip_runs and (only is None or "runs" in only):
+        make_runs(paths, [n for n in model_specs() if n != "bar_phasor"])
+
+
+if __name__ == "__main__":
+    main()

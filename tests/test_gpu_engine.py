@@ -1,0 +1,156 @@
+"""GPU engine behaviour through the C ABI: determinism, independence from the launch shape,
+the ModelSimulator seam, output files, counters and the step loop's bookkeeping."""
+import os
+import re
+import shutil
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, model_path
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api(gpu):
+    from psim_gb300 import api
+    return api
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_same_seed_same_tallies(api, precision):
+    m = api.Model(model_path("kinked_small"))
+    m.run(seed=5, precision=precision)
+    e1, f1 = m.tallies()
+    s1 = m.measurements()
+    m.run(seed=5, precision=precision)
+    e2, f2 = m.tallies()
+    assert np.array_equal(e1, e2) and np.array_equal(f1, f2)
+    assert np.array_equal(s1, m.measurements())
+    m.run(seed=6, precision=precision)
+    e3, _ = m.tallies()
+    assert not np.array_equal(e1, e3)
+
+
+def test_launch_shape_does_not_change_results(api, monkeypatch):
+    """Each phonon's random stream is keyed by its id and step, so the grid size (which
+    reorders the buffer) cannot change any tally."""
+    m = api.Model(model_path("bar_ss"))
+    m.run(seed=9)
+    ref = m.tallies()
+    for grid in ("7", "301"):
+        monkeypatch.setenv("PSIM_GB300_GRID", grid)
+        m2 = api.Model(model_path("bar_ss"))
+        m2.run(seed=9)
+        got = m2.tallies()
+        assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1]), grid
+
+
+def test_counters_and_phonon_steps(api):
+    m = api.Model(model_path("bar_ss"))
+    m.run(seed=3)
+    c = m.counters()
+    assert c["phonons"] > 90000
+    assert c["phonon_steps"] > c["phonons"]
+    assert c["kernel_launches"] >= 1000
+    assert c["max_population"] > 0
+    assert c["kernel_ms"] > 0
+    # SS records the last 10 % of steps: every tallied phonon-step adds its sign; the net
+    # count can never exceed the phonon-steps taken
+    e, _ = m.tallies()
+    assert np.abs(e).sum() <= c["phonon_steps"]
+
+
+def test_seam_matches_model_statistically(api):
+    """psim_sim_* driven directly (the ModelSimulator seam) with the model's own description
+    and emitter energies taken from the reference's tables gives the reference's result."""
+    gold_t = np.load(os.path.join(GOLDEN, "tables_bar_ss.npz"))
+    gold_r = np.load(os.path.join(GOLDEN, "runs_bar_ss.npz"))["stats"]
+    m = api.Model(model_path("bar_ss"))
+    d = m.sim_desc()
+    sim = api.Simulator(d)
+    idesc = m.interp_desc()
+    E = d.n_emitters
+    temps = gold_t["temps"]
+    lines = np.ctypeslib.as_array(d.emit_line, shape=(E, 4))
+    et = np.ctypeslib.as_array(d.emit_temp, shape=(E,))
+    dur = np.ctypeslib.as_array(d.emit_duration, shape=(E,))
+    t_eq = idesc.t_eq
+    emit = np.zeros(E)
+    for e in range(E):
+        k = int(np.searchsorted(temps, et[e]))
+        length = np.hypot(lines[e, 2] - lines[e, 0], lines[e, 3] - lines[e, 1])
+        emit[e] = gold_t["emit_sum"][k] * dur[e] * length / 4.0 * abs(t_eq - et[e])
+    cell = np.zeros(d.n_cells)  # the sensors start at t_eq: no initial phonons
+    S = d.n_sensors
+    init_t = np.ctypeslib.as_array(idesc.sensor_init_temp, shape=(S,)).copy()
+    eff = idesc.eff_energy
+    out = []
+    for seed in range(1, 17):
+        sim.reset()
+        n = sim.init_phonon_builders(t_eq, eff, cell, emit, init_t, seed)
+        assert n > 0
+        sim.run(t_eq)
+        energy, flux = sim.tallies()
+        _, _, stats = api.interpret(idesc, energy, flux)
+        out.append(stats)
+    got = np.stack(out)
+    # the seam applies no post-run energy rescaling (that is Model's job), so compare the
+    # temperature rise profile shape: ordered along the bar like the reference's
+    t_got = got[:, :, 0].mean(axis=0)
+    t_ref = gold_r[:, :, 0].mean(axis=0)
+    assert np.all(np.diff(t_got) < 0) and np.all(np.diff(t_ref) < 0)
+    assert np.corrcoef(t_got, t_ref)[0, 1] > 0.99
+
+
+def test_export_writes_reference_format(api):
+    with tempfile.TemporaryDirectory() as td:
+        for name, prefix, kind in (("bar_ss", "ss_", "Steady State"), ("bar_periodic", "per_", "Periodic"),
+                                   ("plate_small", "per_", "Periodic")):
+            p = os.path.join(td, name + ".json")
+            shutil.copy(model_path(name), p)
+            m = api.Model(p)
+            m.run(seed=1)
+            m.export(p, 1.5)
+            text = open(os.path.join(td, prefix + name + ".txt")).read().splitlines()
+            assert re.match(rf'^{kind} Results from "{name}\.json" @ \d{{4}}-\d\d-\d\d \d\d:\d\d:\d\d - Time Taken 1\.5\[s\] over 1 runs$', text[0])
+            if prefix == "ss_":
+                assert len(text) == 1 + m.n_sensors
+                vals = np.array([[float(v) for v in line.split()] for line in text[1:]])
+                assert vals.shape == (m.n_sensors, 6)
+                assert np.allclose(vals, m.measurements(), rtol=1e-5)
+            else:
+                interval = 25 if name == "bar_periodic" else 20
+                blocks = m.n_recorded // interval
+                assert len(text) == 1 + blocks * (2 + m.n_sensors)
+                assert int(text[1]) == interval // 2 and int(text[2]) == m.n_sensors
+                temps, fluxes = m.series(0)
+                first = np.array([float(v) for v in text[3].split()])
+                assert np.allclose(first, [temps[0, :interval].mean(), fluxes[0, :interval, 0].mean(),
+                                           fluxes[0, :interval, 1].mean()], rtol=1e-5)
+
+
+def test_transient_pulse_spreads_and_conserves(api):
+    """Plate with a 20 ps pulse: energy enters only during the pulse, then only moves."""
+    m = api.Model(model_path("plate_small"))
+    m.run(seed=2)
+    temps, _ = m.series(0)
+    e, _ = m.tallies()
+    total = e.sum(axis=0)
+    # after the pulse there are no absorbing surfaces: the net count is constant
+    assert np.all(total[30:] == total[30])
+    # heat reaches the far side later than the near side
+    near = temps[0:4, :].mean(axis=0)
+    far = temps[-4:, :].mean(axis=0)
+    assert near[:100].max() > far[:100].max()
+
+
+def test_phasor_mode_runs(api):
+    m = api.Model(model_path("bar_phasor"))
+    m.run(seed=4)
+    c = m.counters()
+    assert c["phonon_steps"] > 0
+    st = m.measurements()
+    assert np.all(np.isfinite(st))

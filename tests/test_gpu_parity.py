@@ -1,0 +1,88 @@
+"""Statistical parity of the GPU Monte Carlo with the reference (tests/golden/runs_*.npz: the
+reference's per-sensor results for 16 seeds).  Random streams differ, so per-sensor mean
+temperature and heat flux are compared over 16 seeds each side, in units of the combined
+standard error sqrt(SE_gpu^2 + SE_ref^2), SE = seed-to-seed standard deviation / sqrt(16).
+
+Pass criterion per model (T, flux x, flux y of every sensor): no |z| above 4.5 and at most
+5 % of the values (at least one allowed) above 3.  With independent z-scores the chance of a
+false failure is below 1 %."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, model_path
+
+pytestmark = pytest.mark.gpu
+
+SEEDS = range(1, 17)
+COLUMNS = {"T": 0, "flux_x": 2, "flux_y": 4}
+
+
+@pytest.fixture(scope="module")
+def api(gpu):
+    from psim_gb300 import api
+    return api
+
+
+def gpu_stats(api, name, precision):
+    m = api.Model(model_path(name))
+    out = []
+    for seed in SEEDS:
+        m.run(seed=1000 + seed, precision=precision)
+        out.append(m.measurements())
+    return np.stack(out)
+
+
+def zscores(a, b):
+    """a, b: [seeds, sensors, 6] -> z [sensors, 3] for T, flux x, flux y."""
+    zs = []
+    for col in COLUMNS.values():
+        ma, mb = a[:, :, col].mean(axis=0), b[:, :, col].mean(axis=0)
+        sa = a[:, :, col].std(axis=0, ddof=1) / np.sqrt(a.shape[0])
+        sb = b[:, :, col].std(axis=0, ddof=1) / np.sqrt(b.shape[0])
+        se = np.sqrt(sa ** 2 + sb ** 2)
+        z = np.where(se > 0, (ma - mb) / np.where(se > 0, se, 1.0), np.where(ma == mb, 0.0, np.inf))
+        zs.append(z)
+    return np.stack(zs, axis=1)
+
+
+def check(z, label):
+    az = np.abs(z)
+    over3 = int((az > 3.0).sum())
+    allowed = max(1, int(0.05 * az.size))
+    print(f"{label}: max |z| {az.max():.2f}, {over3}/{az.size} above 3")
+    assert az.max() < 4.5, (label, az.max())
+    assert over3 <= allowed, (label, over3)
+
+
+@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "bar_periodic", "kinked_small", "plate_small", "bar_runs"])
+def test_fp32_matches_reference(api, name):
+    ref = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))["stats"]
+    got = gpu_stats(api, name, api.FP32)
+    check(zscores(got, ref), f"{name} fp32")
+
+
+@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "kinked_small", "plate_small"])
+def test_fp64_matches_reference(api, name):
+    ref = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))["stats"]
+    got = gpu_stats(api, name, api.FP64)
+    check(zscores(got, ref), f"{name} fp64")
+
+
+@pytest.mark.parametrize("name", ["bar_ss", "kinked_small"])
+def test_fp32_error_against_fp64_same_stream(api, name):
+    """The FP32 kernel's error, measured against the FP64 kernel on the same random stream:
+    per-sensor differences stay well inside the statistical noise."""
+    m = api.Model(model_path(name))
+    d32 = []
+    d64 = []
+    for seed in range(1, 9):
+        d32.append(m.run(seed=seed, precision=api.FP32).measurements())
+        d64.append(m.run(seed=seed, precision=api.FP64).measurements())
+    d32, d64 = np.stack(d32), np.stack(d64)
+    ref = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))["stats"]
+    noise = ref[:, :, 0].std(axis=0, ddof=1)
+    diff = np.abs(d32[:, :, 0] - d64[:, :, 0])
+    print(f"{name}: |T32 - T64| mean {diff.mean():.3e} K, max {diff.max():.3e} K; run-to-run noise {noise.mean():.3e} K")
+    assert diff.mean() < 0.5 * noise.mean()

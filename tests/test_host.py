@@ -1,0 +1,219 @@
+"""Host side of libpsim_gb300 without a GPU: the C ABI's exports, model loading and
+validation (the reference's InputManager / Model::addCell / setEmitSurface rules), the
+material tables it builds (bit-exact with the reference's), and that every GPU entry point
+fails loudly when no device is present."""
+import json
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT, model_path
+
+
+@pytest.fixture(scope="module")
+def api(built):
+    from psim_gb300 import api
+    return api
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "psim_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(psim_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(api):
+    declared = header_symbols()
+    assert len(declared) >= 25
+    out = subprocess.run(["nm", "-D", "--defined-only", api.lib_path()], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (psim_[a-z0-9_]+)$", out, flags=re.M))
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    # and the ctypes table covers the same set
+    assert sorted(api.SIGNATURES) == declared
+    for name in declared:
+        assert getattr(api.lib(), name) is not None
+
+
+def test_model_shape(api):
+    m = api.Model(model_path("bar_ss"))
+    assert (m.n_sensors, m.n_cells, m.n_steps, m.n_recorded, m.n_runs) == (10, 20, 1000, 100, 1)
+    k = api.Model(model_path("kinked_small"))
+    assert k.n_sensors == 64 and k.n_cells == 129 and k.n_recorded == 400
+    p = api.Model(model_path("plate_small"))
+    assert p.n_sensors == 64 and p.n_cells == 128 and p.n_recorded == 400
+    d = p.sim_desc()
+    assert d.n_emitters == 2 and d.sim_type == 2
+
+
+def test_topology_of_bar(api):
+    """Transition surfaces on every shared edge, emitters on the two ends (cell.cpp:81-98)."""
+    m = api.Model(model_path("bar_ss"))
+    d = m.sim_desc()  # arrays point into m, which must stay alive
+    C = d.n_cells
+    begin = np.ctypeslib.as_array(d.edge_sub_begin, shape=(3 * C + 1,))
+    kind = np.ctypeslib.as_array(d.sub_kind, shape=(d.n_subs,))
+    assert (kind == 0).sum() == 2 * 19  # 10 diagonals + 9 shared rectangle edges, both sides
+    assert (kind == 1).sum() == 2
+    edge_cell = np.ctypeslib.as_array(d.emit_cell, shape=(2,))
+    assert set(edge_cell.tolist()) == {0, 19}
+    assert begin[-1] == d.n_subs
+
+
+@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "kinked_small"])
+def test_tables_match_reference(api, name):
+    """The cumulative tables handed to the GPU equal the reference's Material tables."""
+    gold = np.load(os.path.join(GOLDEN, f"tables_{name}.npz"))
+    m = api.Model(model_path(name))
+    d = m.sim_desc()
+    tabs = m.tables()
+    temps = gold["temps"]
+    keep = list(gold["keep"])
+    S = d.n_sensors
+    st = np.ctypeslib.as_array(d.sensor_temp, shape=(S,))
+    base_idx = np.ctypeslib.as_array(d.sensor_base_table, shape=(S,))
+    scat_idx = np.ctypeslib.as_array(d.sensor_scatter_table, shape=(S,))
+    exact = os.uname().machine == "x86_64"
+
+    def same(a, b):
+        a = np.nan_to_num(a, nan=-1.0)
+        b = np.nan_to_num(b, nan=-1.0)
+        return np.array_equal(a, b) if exact else np.allclose(a, b, rtol=1e-12, atol=0)
+
+    checked = 0
+    for s in range(S):
+        ti = int(np.searchsorted(temps, st[s]))
+        if ti in keep:
+            k = keep.index(ti)
+            assert same(tabs[base_idx[s]], gold["base"][k])
+            assert same(tabs[scat_idx[s]], gold["scatter"][k])
+            checked += 1
+    E = d.n_emitters
+    et = np.ctypeslib.as_array(d.emit_temp, shape=(E,))
+    ei = np.ctypeslib.as_array(d.emit_table, shape=(E,))
+    for e in range(E):
+        ti = int(np.searchsorted(temps, et[e]))
+        if ti in keep:
+            assert same(tabs[ei[e]], gold["emit"][keep.index(ti)])
+            checked += 1
+    assert checked > 0
+    freq = np.ctypeslib.as_array(d.mat_freq, shape=(1000,))
+    vel = np.ctypeslib.as_array(d.mat_vel, shape=(2, 1000))
+    assert same(freq, gold["freq"]) and same(vel[0], gold["vel_la"]) and same(vel[1], gold["vel_ta"])
+    idesc = m.interp_desc()
+    n = idesc.mat_temp_begin[1]
+    assert np.array_equal(np.ctypeslib.as_array(idesc.temps, shape=(n,)), temps)
+    assert same(np.ctypeslib.as_array(idesc.energies, shape=(n,)), gold["base_sum"])
+    assert (idesc.lower_bound, idesc.upper_bound) == tuple(gold["bounds"])
+
+
+@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "kinked_small"])
+def test_energy_per_phonon_matches_reference(api, name):
+    """Model::getTotalInitialEnergy / num_phonons (model.cpp:148-155,196-201)."""
+    gold = np.load(os.path.join(GOLDEN, f"invert_{name}.npz"))
+    m = api.Model(model_path(name))
+    eff = m.interp_desc().eff_energy
+    if os.uname().machine == "x86_64":
+        assert eff == float(gold["eff"])
+    else:
+        assert eff == pytest.approx(float(gold["eff"]), rel=1e-12)
+
+
+def _write(tmp, model):
+    p = os.path.join(tmp, "m.json")
+    with open(p, "w") as f:
+        json.dump(model, f)
+    return p
+
+
+def test_validation_errors(api):
+    from psim_gb300 import modelgen as mg
+    with tempfile.TemporaryDirectory() as td:
+        base = mg.bar(num_cells=3, num_phonons=1000, num_measurements=100, sim_time=1.0)
+        # degenerate triangle (TriangleError)
+        m = json.loads(json.dumps(base))
+        m["cells"][0]["triangle"]["p2"] = dict(m["cells"][0]["triangle"]["p1"])
+        with pytest.raises(api.PsimError, match="valid triangle"):
+            api.Model(_write(td, m))
+        # duplicate cell: found when the copy is checked against itself after the original
+        # (model.cpp:102-111); a copy added later first collides with the original's
+        # transition surfaces, as in the reference
+        m = json.loads(json.dumps(base))
+        m["cells"].insert(0, dict(m["cells"][0]))
+        with pytest.raises(api.PsimError, match="Duplicate cell"):
+            api.Model(_write(td, m))
+        m = json.loads(json.dumps(base))
+        m["cells"].append(dict(m["cells"][0]))
+        with pytest.raises(api.PsimError, match="conflicts"):
+            api.Model(_write(td, m))
+        # overlapping cell (IntersectError)
+        m = json.loads(json.dumps(base))
+        m["cells"].append({"triangle": {"p1": {"x": 10.0, "y": 10.0}, "p2": {"x": 10.0, "y": 150.0},
+                                        "p3": {"x": 150.0, "y": 10.0}}, "sensorID": 0, "specularity": 0.0})
+        with pytest.raises(api.PsimError, match="intersects|contained"):
+            api.Model(_write(td, m))
+        # emitting surface that lies on no cell edge
+        m = json.loads(json.dumps(base))
+        m["emit_surfaces"].append({"p1": {"x": 50.0, "y": 20.0}, "p2": {"x": 50.0, "y": 80.0}, "temp": 300.0,
+                                   "duration": 1.0, "start_time": 0.0, "length": 1.0})
+        with pytest.raises(api.PsimError, match="emitting surface|conflicts"):
+            api.Model(_write(td, m))
+        # transient emitter in a steady-state model
+        m = json.loads(json.dumps(base))
+        m["emit_surfaces"][0]["duration"] = 0.5
+        with pytest.raises(api.PsimError, match="non transient"):
+            api.Model(_write(td, m))
+        # unknown sensor
+        m = json.loads(json.dumps(base))
+        m["cells"][0]["sensorID"] = 99
+        with pytest.raises(api.PsimError, match="Sensor does not exist"):
+            api.Model(_write(td, m))
+        # steady state with a step interval
+        m = json.loads(json.dumps(base))
+        m["settings"]["step_interval"] = 5
+        api.Model(_write(td, m))  # the reference ignores step_interval for sim_type 0 (inputManager.cpp:81-82)
+        # transient in full mode
+        m = json.loads(json.dumps(base))
+        m["settings"]["sim_type"] = 2
+        m["settings"]["step_interval"] = 5
+        m["settings"]["t_eq"] = 0.0
+        with pytest.raises(api.PsimError, match="deviational"):
+            api.Model(_write(td, m))
+        with pytest.raises(api.PsimError) as e:
+            api.Model(os.path.join(td, "missing.json"))
+        assert e.value.code == api.PSIM_ERR_IO
+        with open(os.path.join(td, "bad.json"), "w") as f:
+            f.write("{ not json")
+        with pytest.raises(api.PsimError, match="JSON"):
+            api.Model(os.path.join(td, "bad.json"))
+
+
+def test_gpu_entry_points_fail_loudly_without_a_device(api):
+    if api.device_count() > 0:
+        pytest.skip("a CUDA device is present")
+    m = api.Model(model_path("bar_ss"))
+    with pytest.raises(api.PsimError) as e:
+        m.run(seed=1)
+    assert e.value.code == api.PSIM_ERR_CUDA
+    with pytest.raises(api.PsimError) as e:
+        api.Simulator(m.sim_desc())
+    assert e.value.code == api.PSIM_ERR_CUDA
+    g = np.load(os.path.join(GOLDEN, "geom.npz"))
+    with pytest.raises(api.PsimError):
+        api.geom_intersect(g["intersect_a"][:4], g["intersect_b"][:4])
+
+
+def test_modelgen_workloads_load(api):
+    from psim_gb300 import modelgen as mg
+    with tempfile.TemporaryDirectory() as td:
+        k = api.Model(mg.write(mg.kinked(num_phonons=1000, num_measurements=100, sim_time=1.0), os.path.join(td, "k.json")))
+        # (k stays alive while its description is read)
+        assert k.n_sensors == 400 and k.n_cells == 801
+        d = k.sim_desc()
+        assert d.n_emitters == 6
+        p = api.Model(mg.write(mg.plate(num_phonons=1000), os.path.join(td, "p.json")))
+        assert p.n_sensors == 1024 and p.n_cells == 2048 and p.sim_desc().n_emitters == 4
