@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../host/geom64.hpp"
+#include "cells.hpp"
 #include "common.cuh"
 
 namespace psim::gpu {
@@ -130,59 +131,13 @@ __global__ void unpack_kernel(const TallySlot* t, std::uint32_t S, std::uint64_t
 
 }// namespace
 
-struct Engine::Impl {
-    Buf cells32, cells64, subs64, sensors, materials, emitters, alias, centre32, vel32, centre64, vel64;
-    std::vector<EmitterDev> emit_host;
-    std::vector<BirthGroup> groups;
-    std::vector<std::uint32_t> group_begin;// [N+1]
-    std::vector<std::uint32_t> n_new;      // [N]
-    std::vector<std::uint32_t> id_base;    // [N]
-    Buf d_groups;
-    Buf state[2];
-    std::uint64_t capacity{ 0 };
-    Buf counts;  // 3 x u32
-    Buf counters;// 8 x u64: phonon-steps, relocations, overflow, max population, event-limit hits
-    Buf tally;   // [K][S]
-    Buf unpacked_energy, unpacked_flux;
-    std::uint64_t total{ 0 };
-    std::uint32_t key0{ 0 }, key1{ 0 };
-    bool builders_ready{ false };
-    cudaEvent_t ev0{ nullptr }, ev1{ nullptr };
-    cudaStream_t own{ nullptr };
-    int sms{ 0 };
-};
-
-int device_count() noexcept {
-    int n = 0;
-    if (cudaGetDeviceCount(&n) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
-}
-
-Engine::Engine(const SimDesc& d)
-    : desc_{ d }
-    , impl_{ std::make_unique<Impl>() } {
-    if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
-    if (d.n_cells == 0 || d.n_sensors == 0 || d.n_materials == 0 || d.steps == 0) { throw std::invalid_argument("empty model"); }
-    if (d.n_materials > kMaxMaterials) { throw std::invalid_argument("at most 16 materials are supported"); }
-    if (d.n_cells >= (1U << 24)) { throw std::invalid_argument("at most 2^24 - 1 cells are supported"); }
-    if (d.steps >= 0xFFFFFFFFULL) { throw std::invalid_argument("too many measurement steps"); }
-    Impl& I = *impl_;
-    int dev = 0;
-    check(cudaGetDevice(&dev), "cudaGetDevice");
-    check(cudaDeviceGetAttribute(&I.sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
-    check(cudaStreamCreateWithFlags(&I.own, cudaStreamNonBlocking), "stream");
-    stream_ = I.own;
-    check(cudaEventCreate(&I.ev0), "event");
-    check(cudaEventCreate(&I.ev1), "event");
-
+// Device cell records from the flattened description: the FP32 cell-local form (outward
+// normals, offsets, edge links, neighbour entry edges) and the FP64 reference form.
+void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF64>& c64, std::vector<Sub64>& subs) {
     const std::uint32_t C = d.n_cells;
-    // ---- cells
-    std::vector<CellF32> c32(C);
-    std::vector<CellF64> c64(C);
-    std::vector<Sub64> subs(d.sub_kind.size());
+    c32.assign(C, CellF32{});
+    c64.assign(C, CellF64{});
+    subs.assign(d.sub_kind.size(), Sub64{});
     auto vtx = [&](std::uint32_t c, int i) {
         return psim::P2{ d.cell_vertices[6 * c + 2 * i], d.cell_vertices[6 * c + 2 * i + 1] };
     };
@@ -260,6 +215,64 @@ Engine::Engine(const SimDesc& d)
             }
         }
     }
+}
+
+struct Engine::Impl {
+    Buf cells32, cells64, subs64, sensors, materials, emitters, alias, centre32, vel32, centre64, vel64;
+    std::vector<EmitterDev> emit_host;
+    std::vector<BirthGroup> groups;
+    std::vector<std::uint32_t> group_begin;// [N+1]
+    std::vector<std::uint32_t> n_new;      // [N]
+    std::vector<std::uint32_t> id_base;    // [N]
+    Buf d_groups;
+    Buf state[2];
+    std::uint64_t capacity{ 0 };
+    Buf counts;  // 3 x u32
+    Buf counters;// 8 x u64: phonon-steps, relocations, overflow, max population, event-limit hits
+    Buf tally;   // [K][S]
+    Buf unpacked_energy, unpacked_flux;
+    std::uint64_t total{ 0 };
+    std::uint32_t key0{ 0 }, key1{ 0 };
+    bool builders_ready{ false };
+    cudaEvent_t ev0{ nullptr }, ev1{ nullptr };
+    cudaStream_t own{ nullptr };
+    int sms{ 0 };
+};
+
+int device_count() noexcept {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+Engine::Engine(const SimDesc& d)
+    : desc_{ d }
+    , impl_{ std::make_unique<Impl>() } {
+    if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
+    if (d.n_cells == 0 || d.n_sensors == 0 || d.n_materials == 0 || d.steps == 0) { throw std::invalid_argument("empty model"); }
+    if (d.n_materials > kMaxMaterials) { throw std::invalid_argument("at most 16 materials are supported"); }
+    if (d.n_cells >= (1U << 24)) { throw std::invalid_argument("at most 2^24 - 1 cells are supported"); }
+    if (d.steps >= 0xFFFFFFFFULL) { throw std::invalid_argument("too many measurement steps"); }
+    Impl& I = *impl_;
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&I.sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    check(cudaStreamCreateWithFlags(&I.own, cudaStreamNonBlocking), "stream");
+    stream_ = I.own;
+    check(cudaEventCreate(&I.ev0), "event");
+    check(cudaEventCreate(&I.ev1), "event");
+
+    std::vector<CellF32> c32;
+    std::vector<CellF64> c64;
+    std::vector<Sub64> subs;
+    build_cells(d, c32, c64, subs);
+    const std::uint32_t C = d.n_cells;
+    auto vtx = [&](std::uint32_t c, int i) {
+        return psim::P2{ d.cell_vertices[6 * c + 2 * i], d.cell_vertices[6 * c + 2 * i + 1] };
+    };
     I.cells32.upload(c32);
     I.cells64.upload(c64);
     I.subs64.upload(subs);

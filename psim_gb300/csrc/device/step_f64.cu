@@ -63,7 +63,7 @@ __device__ __forceinline__ void diffuse_dir(Ph64& p, Stream& rs, double nx, doub
 
 // Surface::boundaryHandlePhonon (psim/src/surface.cpp:32-44); (nx, ny) is the inward normal.
 __device__ __forceinline__ void reflect(Ph64& p, Stream& rs, double spec, double nx, double ny) {
-    if (spec == 1. || rs.ud() < spec) {
+    if (spec >= 1. || (spec > 0. && rs.ud() < spec)) {// a draw only when the choice is random (as the FP32 kernel)
         const double ndx = -p.dx * nx - p.dy * ny;
         const double ndy = -p.dx * ny + p.dy * nx;
         p.dx = nx * ndx - ny * ndy;

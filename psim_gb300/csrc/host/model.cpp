@@ -507,17 +507,9 @@ void HostModel::run() {
         if (fresh) { engine_ = std::make_unique<gpu::Engine>(desc_); }
         engine_->reset();
         if (fresh) { engine_->add_h2d(engine_->model_bytes()); }
-        std::vector<double> cell_energy(cells_.size());
-        std::vector<double> emit_energy(emitters_.size());
-        for (std::size_t c = 0; c < cells_.size(); ++c) { cell_energy[c] = cell_init_energy(c); }
-        for (std::size_t e = 0; e < emitters_.size(); ++e) {// ModelSimulator::initPhononBuilders emitter energy
-            const EmitterRec& em = emitters_[e];
-            const MaterialTables& m = mats_[sensors_[cells_[em.cell].sensor].material];
-            const double factor = m.emit(m.temp_index(em.temp)).sum * em.duration * em.length / 4.;
-            emit_energy[e] = (t_eq_ == 0.) ? factor : factor * std::fabs(t_eq_ - em.temp);
-        }
-        std::vector<double> sensor_t0(sensors_.size());
-        for (std::size_t s = 0; s < sensors_.size(); ++s) { sensor_t0[s] = init_temp(sensors_[s]); }
+        const std::vector<double> cell_energy = cell_energies();
+        const std::vector<double> emit_energy = emit_energies();
+        const std::vector<double> sensor_t0 = sensor_init_temps();
         const std::uint64_t run_seed = seed_ * 0x9E3779B97F4A7C15ULL + run * 0xD1B54A32D192ED03ULL + 1;
         engine_->init_builders(t_eq_, eff_energy_, cell_energy.data(), emit_energy.data(), sensor_t0.data(), run_seed);
         engine_->run(precision_, stream_);
@@ -544,6 +536,29 @@ void HostModel::run() {
         for (auto& s : sensors_) { s.t_steady = s.t_init; }// Model::reset(true) before the next run
     }
     last_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+std::vector<double> HostModel::cell_energies() const {
+    std::vector<double> out(cells_.size());
+    for (std::size_t c = 0; c < cells_.size(); ++c) { out[c] = cell_init_energy(c); }
+    return out;
+}
+
+std::vector<double> HostModel::emit_energies() const {// ModelSimulator::initPhononBuilders: modelSimulator.cpp:66-70
+    std::vector<double> out(emitters_.size());
+    for (std::size_t e = 0; e < emitters_.size(); ++e) {
+        const EmitterRec& em = emitters_[e];
+        const MaterialTables& m = mats_[sensors_[cells_[em.cell].sensor].material];
+        const double factor = m.emit(m.temp_index(em.temp)).sum * em.duration * em.length / 4.;
+        out[e] = (t_eq_ == 0.) ? factor : factor * std::fabs(t_eq_ - em.temp);
+    }
+    return out;
+}
+
+std::vector<double> HostModel::sensor_init_temps() const {
+    std::vector<double> out(sensors_.size());
+    for (std::size_t s = 0; s < sensors_.size(); ++s) { out[s] = init_temp(sensors_[s]); }
+    return out;
 }
 
 std::vector<std::array<double, 6>> HostModel::averaged() const {// OutputManager::calculateAverages

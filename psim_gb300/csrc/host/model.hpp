@@ -98,6 +98,13 @@ public:
     // Interpreter description with the given energy per phonon (<= 0: initial total energy / phonons).
     gpu::InterpDesc interp_for(double eff) const { return interp_desc(eff > 0. ? eff : initial_eff_); }
     gpu::Engine* engine() const noexcept { return engine_.get(); }
+    // Energies ModelSimulator::initPhononBuilders turns into phonon counts (cell.cpp:38-41,
+    // modelSimulator.cpp:66-70), for the current sensor temperatures.
+    std::vector<double> cell_energies() const;
+    std::vector<double> emit_energies() const;
+    std::vector<double> sensor_init_temps() const;
+    double t_eq() const noexcept { return t_eq_; }
+    double initial_eff_energy() const noexcept { return initial_eff_; }
 
 private:
     HostModel() = default;

@@ -146,6 +146,8 @@ def _arm_grid(origin: Point, angle_deg: float, length: float, width: float, n_le
     ``angle_deg``; node[i][j] is i steps along the arm and j steps across it."""
     a = math.radians(angle_deg)
     ux, uy = math.cos(a), math.sin(a)
+    if angle_deg % 90.0 == 0.0:  # exact unit vectors for right angles
+        ux, uy = float(round(ux)), float(round(uy))
     vx, vy = -uy, ux
     nodes = []
     for i in range(n_len + 1):
@@ -171,7 +173,11 @@ def kinked(*, seed: int = 0, arm_length: float = 2000.0, width: float = 200.0, n
     rng = random.Random(seed)
     b = Builder(num_measurements=num_measurements, sim_time=sim_time, num_phonons=num_phonons, t_eq=t_eq,
                 sim_type=sim_type, step_interval=step_interval)
-    centre = (0.0, 0.0)
+    # The hub sits well away from the origin: psim's geometry tests a line for being vertical
+    # with a tolerance relative to its x coordinates (psim/src/geometry.cpp:107-109) but takes
+    # its slope with an absolute one (:325-327), so a vertical edge at |x| of order 1e-13 nm
+    # would be intersected as if it were horizontal.
+    centre = (3000.0, 3000.0)
     r0 = 150.0
     angles = (180.0, 90.0, -45.0)
     arms = [_arm_grid(centre, ang, arm_length, width, n_len, n_wid, r0) for ang in angles]
