@@ -188,7 +188,8 @@ def main():
     ap.add_argument("--per-step", type=float, default=PER_STEP)
     ap.add_argument("--measurements", type=int, default=STEPS)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
-    ap.add_argument("--cpu-budget", type=int, default=200000)
+    ap.add_argument("--cpu-budget", type=int, default=3000000)
+    ap.add_argument("--population-out", default="", help="write the phonon population per step of the last timed run (JSON)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -239,6 +240,10 @@ def main():
     ev1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    if args.population_out:
+        with open(args.population_out, "w") as f:
+            json.dump({"population": model.population().tolist(), "pilot_runs": 1, "warmup_runs": args.warmup,
+                       "timed_runs": args.steps, "steps_per_run": steps_n}, f)
     clk = clocks.stop(local)
     barrier(dist)
     span_ms = ev0.elapsed_time(ev1)

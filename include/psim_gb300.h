@@ -89,6 +89,8 @@ int psim_model_series(const psim_model* m, int64_t run, double* temps, double* f
  * (sum of sign * velocity, m/s) as Sensor::inc_energy_ / inc_flux_ (psim/src/sensor.cpp:43-52). */
 int psim_model_tallies(const psim_model* m, int64_t* energy, double* flux);
 int psim_model_counters(const psim_model* m, psim_run_counters* out);
+/* Phonons in flight (alive plus newly born) at each measurement step of the last run: out[n_steps]. */
+int psim_model_population(const psim_model* m, uint32_t* out);
 /* Forward declarations of the seam descriptions (defined below). */
 struct psim_sim_desc;
 struct psim_interp_desc;
@@ -188,6 +190,8 @@ int psim_sim_set_step_adjustment(psim_sim* s, uint64_t step_adjustment);
 /* energy[S][K] and flux[S][K][2] as in psim_model_tallies. */
 int psim_sim_tallies(const psim_sim* s, int64_t* energy, double* flux);
 int psim_sim_counters(const psim_sim* s, psim_run_counters* out);
+/* Phonons in flight at each measurement step of the last run: out[measurement_steps]. */
+int psim_sim_population(const psim_sim* s, uint32_t* out);
 void psim_sim_destroy(psim_sim* s);
 
 /* ------------------------------------------------------------------------------------------

@@ -92,6 +92,8 @@ SIGNATURES = {
     "psim_model_series": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_dp, _c_dp]),
     "psim_model_tallies": (ctypes.c_int, [ctypes.c_void_p, _c_i64p, _c_dp]),
     "psim_model_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RunCounters)]),
+    "psim_model_population": (ctypes.c_int, [ctypes.c_void_p, _c_u32p]),
+    "psim_sim_population": (ctypes.c_int, [ctypes.c_void_p, _c_u32p]),
     "psim_model_sim_desc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SimDesc)]),
     "psim_model_interp_desc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.POINTER(InterpDesc)]),
     "psim_model_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double]),
@@ -215,6 +217,12 @@ class Model:
         _check(lib().psim_model_counters(self._h, ctypes.byref(c)))
         return c.as_dict()
 
+    def population(self) -> np.ndarray:
+        """Phonons in flight at each measurement step of the last run."""
+        out = np.zeros(self.n_steps, dtype=np.uint32)
+        _check(lib().psim_model_population(self._h, out.ctypes.data_as(_c_u32p)))
+        return out
+
     def export(self, json_path: Optional[str] = None, seconds: float = 0.0) -> None:
         _check(lib().psim_model_export(self._h, (json_path or self.path).encode(), seconds))
 
@@ -283,6 +291,11 @@ class Simulator:
         c = RunCounters()
         _check(lib().psim_sim_counters(self._h, ctypes.byref(c)))
         return c.as_dict()
+
+    def population(self) -> np.ndarray:
+        out = np.zeros(self.desc.measurement_steps, dtype=np.uint32)
+        _check(lib().psim_sim_population(self._h, out.ctypes.data_as(_c_u32p)))
+        return out
 
 
 def interpret(desc: InterpDesc, energy: np.ndarray, flux: np.ndarray):

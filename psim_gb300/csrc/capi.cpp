@@ -146,6 +146,12 @@ int psim_model_counters(const psim_model* m, psim_run_counters* out) {
     return PSIM_OK;
 }
 
+int psim_model_population(const psim_model* m, uint32_t* out) {
+    if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    if (m->m->engine() == nullptr) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
+    return guard([&]() { m->m->engine()->population(out); });
+}
+
 int psim_model_export(const psim_model* m, const char* json_path, double seconds) {
     if (m == nullptr || json_path == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     if (m->m->measurements().empty()) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
@@ -319,6 +325,11 @@ int psim_sim_counters(const psim_sim* s, psim_run_counters* out) {
     out->h2d_bytes = c.h2d_bytes;
     out->d2h_bytes = c.d2h_bytes;
     return PSIM_OK;
+}
+
+int psim_sim_population(const psim_sim* s, uint32_t* out) {
+    if (s == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    return guard([&]() { s->e->population(out); });
 }
 
 void psim_sim_destroy(psim_sim* s) { delete s; }

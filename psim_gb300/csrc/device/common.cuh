@@ -83,13 +83,14 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, std::uint32_t k0, std::uint32_
     return c;
 }
 
-// Per-phonon stream for one step: four 32-bit words per Philox call, refilled on demand.
+// Per-phonon stream for one step: four 32-bit words per Philox call, refilled on demand.  The
+// words shift through registers (no indexed array, so nothing spills to local memory).
 struct Stream {
     std::uint32_t k0, k1;
     std::uint32_t step, id;
     std::uint32_t block;
-    std::uint32_t buf[4];
-    int used;
+    std::uint32_t b0, b1, b2, b3;
+    int left;
 
     __device__ __forceinline__ void init(std::uint32_t key0, std::uint32_t key1, std::uint32_t s, std::uint32_t pid) {
         k0 = key0;
@@ -97,19 +98,24 @@ struct Stream {
         step = s;
         id = pid;
         block = 0;
-        used = 4;
+        left = 0;
     }
     __device__ __forceinline__ std::uint32_t next() {
-        if (used == 4) {
+        if (left == 0) {
             const U4 r = philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
-            buf[0] = r.x;
-            buf[1] = r.y;
-            buf[2] = r.z;
-            buf[3] = r.w;
+            b0 = r.x;
+            b1 = r.y;
+            b2 = r.z;
+            b3 = r.w;
             ++block;
-            used = 0;
+            left = 4;
         }
-        return buf[used++];
+        const std::uint32_t out = b0;
+        b0 = b1;
+        b1 = b2;
+        b2 = b3;
+        --left;
+        return out;
     }
     // Uniform in the open interval (0, 1), 24-bit resolution.
     __device__ __forceinline__ float uf() { return (static_cast<float>(next() >> 8) + 0.5f) * 5.9604644775390625e-8f; }
@@ -229,6 +235,9 @@ struct StepParams {
     const std::uint32_t* count_in;
     std::uint32_t* count_out;
     std::uint32_t* count_clear;
+    std::uint32_t* work;              // this step's work counter (phonons handed to lanes)
+    std::uint32_t* work_clear;        // the counter of two steps ahead, cleared by this step
+    std::uint32_t* population;        // [n_steps] phonons in flight per step (may be null)
     // step
     std::uint32_t step;               // 0-based step index; phonons alive at its end reach boundary step+1
     std::uint32_t n_steps;

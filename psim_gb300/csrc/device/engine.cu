@@ -230,6 +230,7 @@ struct Engine::Impl {
     Buf counts;  // 3 x u32
     Buf counters;// 8 x u64: phonon-steps, relocations, overflow, max population, event-limit hits
     Buf tally;   // [K][S]
+    Buf population;// [N] u32
     Buf unpacked_energy, unpacked_flux;
     std::uint64_t total{ 0 };
     std::uint32_t key0{ 0 }, key1{ 0 };
@@ -385,9 +386,11 @@ Engine::Engine(const SimDesc& d)
     model_bytes_ = I.cells32.bytes + I.cells64.bytes + I.subs64.bytes + I.materials.bytes + I.centre32.bytes + I.vel32.bytes
                    + I.centre64.bytes + I.vel64.bytes + I.alias.bytes + I.sensors.bytes + I.emitters.bytes;
     // ---- run buffers
-    I.counts.alloc(4 * sizeof(std::uint32_t));
+    I.counts.alloc(8 * sizeof(std::uint32_t));// 3 survivor counters, 3 work counters
     I.counters.alloc(8 * sizeof(unsigned long long));
     I.tally.alloc(static_cast<std::size_t>(d.recorded) * d.n_sensors * sizeof(TallySlot));
+    I.population.alloc(static_cast<std::size_t>(d.steps) * sizeof(std::uint32_t));
+    check(cudaMemset(I.population.p, 0, I.population.bytes), "memset population");
     check(cudaMemset(I.tally.p, 0, I.tally.bytes), "memset tally");
 }
 
@@ -541,6 +544,7 @@ void Engine::run(int precision, void* stream_ptr) {
     P.key1 = I.key1;
     P.tally = I.tally.as<TallySlot>();
     P.counters = I.counters.as<unsigned long long>();
+    P.population = I.population.as<std::uint32_t>();
     auto* counts = I.counts.as<std::uint32_t>();
     const int occ = std::max(1, fp64 ? occupancy_f64() : occupancy_f32());
     int grid = grid_override_ > 0 ? grid_override_ : I.sms * occ;
@@ -554,6 +558,8 @@ void Engine::run(int precision, void* stream_ptr) {
             P.count_in = counts + (s % 3);
             P.count_out = counts + ((s + 1) % 3);
             P.count_clear = counts + ((s + 2) % 3);
+            P.work = counts + 4 + (s % 3);
+            P.work_clear = counts + 4 + ((s + 2) % 3);
             P.group_begin = I.group_begin[s];
             P.group_end = I.group_begin[s + 1];
             P.n_new = I.n_new[s];
@@ -623,6 +629,12 @@ void unpack(const Engine& eng, Buf& e, Buf& f, cudaStream_t stream, const void* 
     }
 }
 }// namespace
+
+void Engine::population(std::uint32_t* out) const {
+    Impl& I = *impl_;
+    check(cudaMemcpy(out, I.population.p, desc_.steps * sizeof(std::uint32_t), cudaMemcpyDeviceToHost), "copy population");
+    counters_.d2h_bytes += desc_.steps * sizeof(std::uint32_t);
+}
 
 void Engine::tallies(std::int64_t* energy, double* flux) const {
     Impl& I = *impl_;

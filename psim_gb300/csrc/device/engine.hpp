@@ -86,6 +86,8 @@ public:
     void set_use_graph(bool on) { use_graph_ = on; }
     void set_grid(int blocks) { grid_override_ = blocks; }
 
+    // Phonons in flight at each measurement step of the last run (alive + born), [steps].
+    void population(std::uint32_t* out) const;
     // Raw tallies (host): energy[S][K], flux[S][K][2].
     void tallies(std::int64_t* energy, double* flux) const;
     // Device-resident interpretation of the current tallies.

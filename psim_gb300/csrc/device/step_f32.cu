@@ -98,7 +98,7 @@ __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream
 
 // Create newborn j of this step (CellOriginBuilder / SurfaceOriginBuilder / PhasorBuilder,
 // psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
-__device__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
+__device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
     const BirthGroup g = P.groups[find_group(P, j)];
     p.id = P.id_base + j;
     rs.init(P.key0, P.key1, P.step, p.id);
@@ -138,6 +138,22 @@ __device__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t
     return fmaxf(P.dt - t_birth, 0.f);
 }
 
+// A phonon in flight on one lane: its state, its random stream and where it is inside the
+// current event (the drift to the next scattering event or step boundary, with the edge
+// impacts on the way).
+struct Lane {
+    Ph32 p;
+    Stream rs;
+    float rem;      // time left until the step boundary (ns)
+    float target;   // length of the current event's drift (ns)
+    float drifted;  // part of it already covered by impacts
+    float v;        // group velocity (m/s = nm/ns)
+    std::uint32_t sensor, mat;
+    int ncoll;      // impacts in the current event (MAX_COLLISIONS rule)
+    unsigned events;
+    bool need_target, changed;
+};
+
 struct Outcome {
     bool alive;
     bool boundary;// reached the step boundary (a phonon-step), alive or at the last boundary
@@ -146,158 +162,188 @@ struct Outcome {
     long long fx, fy;
 };
 
-// Events of one phonon until the step boundary (or absorption).
-__device__ Outcome transport32(const StepParams& P, Ph32& p, Stream& rs, float rem, unsigned long long& relocations,
-                               unsigned long long& limits) {
-    Outcome out{ false, false, false, 0U, 0, 0 };
-    std::uint32_t cell = meta_cell(p.meta);
-    const CellF32* C = P.cells32 + cell;
-    std::uint32_t sensor = C->sensor;
-    std::uint32_t mat = C->material;
+__device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive,
+                                           const float4* in_pd, const uint4* in_meta) {
+    if (i < n_alive) {
+        const float4 a = in_pd[i];
+        const uint4 b = in_meta[i];
+        L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
+        L.rs.init(P.key0, P.key1, P.step, L.p.id);
+        L.rem = P.dt;
+    } else {
+        L.rem = spawn32(P, L.p, L.rs, i - n_alive);
+    }
+    const CellF32* C = P.cells32 + meta_cell(L.p.meta);
+    L.sensor = C->sensor;
+    L.mat = C->material;
+    L.v = vel32(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
+    L.need_target = true;
+    L.events = 0;
+}
+
+// One segment of a phonon's step: the straight flight to the next edge impact or to the end of
+// the current event (ModelSimulator::simulatePhonon / handleImpacts / nextImpact,
+// psim/src/modelSimulator.cpp:87-225).  Returns true when the phonon's step is over (it
+// reached the step boundary or was absorbed); the outcome says which.
+__device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out, unsigned long long& relocations,
+                          unsigned long long& limits) {
+    Ph32& p = L.p;
+    Stream& rs = L.rs;
     const bool phasor = meta_phasor(p.meta);
-    int pol = meta_pol(p.meta);
-    float v = vel32(P, p.binw, pol, phasor);
-    unsigned events = 0;
-    while (true) {
-        if (++events > kMaxEventsPerStep) {// numerical corner case: end the step where the phonon is
+    if (L.need_target) {
+        if (++L.events > kMaxEventsPerStep) {// numerical corner case: end the step where the phonon is
             ++limits;
-            rem = 0.f;
+            L.rem = 0.f;
             p.tts = fmaxf(p.tts, 0.f);
         }
-        if (p.tts <= 0.f) {// draw the time to the next scattering event (modelSimulator.cpp:148-153)
-            const float3 r = rates32(P.materials[mat], P.sensors[sensor], omega32(P, p.binw, phasor), pol);
+        if (p.tts <= 0.f) {// time to the next scattering event (modelSimulator.cpp:148-153)
+            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), meta_pol(p.meta));
             p.tts = 1e9f * (-__logf(rs.uf())) / (r.x + r.y + r.z);
         }
-        const bool meas = rem <= p.tts;
-        const float target = meas ? rem : p.tts;
-        float drifted = 0.f;
-        int ncoll = 0;
-        bool changed = false;
-        while (true) {// handleImpacts / nextImpact (modelSimulator.cpp:87-122, 205-225)
-            const float wx = p.dx * v;
-            const float wy = p.dy * v;
-            const std::uint32_t entry = meta_edge(p.meta);
-            float tbest = 3.0e38f;
-            int ebest = -1;
+        L.target = (L.rem <= p.tts) ? L.rem : p.tts;
+        L.drifted = 0.f;
+        L.ncoll = 0;
+        L.changed = false;
+        L.need_target = false;
+    }
+    std::uint32_t cell = meta_cell(p.meta);
+    const CellF32* C = P.cells32 + cell;
+    const float wx = p.dx * L.v;
+    const float wy = p.dy * L.v;
+    const std::uint32_t entry = meta_edge(p.meta);
+    float tbest = 3.0e38f;
+    int ebest = -1;
 #pragma unroll
-            for (int e = 0; e < 3; ++e) {
-                const float4 E = C->edge[e];
-                const float den = E.x * wx + E.y * wy;
-                if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
-                    const float t = fmaxf((E.z - (E.x * p.px + E.y * p.py)) / den, 0.f);
-                    if (t < tbest) {
-                        tbest = t;
-                        ebest = e;
-                    }
-                }
+    for (int e = 0; e < 3; ++e) {
+        const float4 E = C->edge[e];
+        const float den = E.x * wx + E.y * wy;
+        if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
+            const float t = fmaxf((E.z - (E.x * p.px + E.y * p.py)) / den, 0.f);
+            if (t < tbest) {
+                tbest = t;
+                ebest = e;
             }
-            const float left = target - drifted;
-            if (ebest < 0 || tbest > left) {
-                p.px += wx * left;
-                p.py += wy * left;
-                drifted = target;
-                break;
-            }
-            p.px += wx * tbest;
-            p.py += wy * tbest;
-            drifted += tbest;
-            const float4 E = C->edge[ebest];
-            const int link = C->link[ebest];
-            std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
-            if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
-                const CellF32* N = P.cells32 + link;
-                bool pass = true;
-                if (N->material != mat) {
-                    const MaterialDev& mt = P.materials[N->material];
-                    const float w = omega32(P, p.binw, phasor);
-                    pass = !(w > (pol == 0 ? mt.w_max_la : mt.w_max_ta));
-                }
-                if (pass) {
-                    p.px += C->offset[ebest].x;
-                    p.py += C->offset[ebest].y;
-                    entry_next = (C->rev >> (2 * ebest)) & 3U;
-                    cell = static_cast<std::uint32_t>(link);
-                    C = N;
-                    if (C->sensor != sensor) {
-                        sensor = C->sensor;
-                        changed = true;
-                    }
-                    mat = C->material;
-                } else {
-                    const float flip = ((C->rev >> (8 + ebest)) & 1U) ? -1.f : 1.f;
-                    diffuse_dir(p, rs, -E.x * flip, -E.y * flip);
-                }
-            } else if (link == -1) {
-                reflect(p, rs, C->spec, E);
-            } else {// EmitSurface::handlePhonon (psim/src/surface.cpp:61-65)
-                const EmitterDev& em = P.emitters[static_cast<std::uint32_t>(-(link + 2))];
-                if (P.step >= em.absorb_lo && P.step <= em.absorb_hi) { return out; }// absorbed
-                reflect(p, rs, C->spec, E);
-            }
-            p.meta = meta_with_cell_edge(p.meta, cell, entry_next);
-            if (++ncoll > kMaxCollisions) {// stuck in a corner: random point in the cell
-                float r1 = rs.uf();
-                float r2 = rs.uf();
-                if (r1 + r2 > 1.f) {
-                    r1 = 1.f - r1;
-                    r2 = 1.f - r2;
-                }
-                p.px = C->vert[1].x * r1 + C->vert[2].x * r2;
-                p.py = C->vert[1].y * r1 + C->vert[2].y * r2;
-                p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
-                drifted = target;
-                ++relocations;
-                break;
-            }
-            if (changed) { break; }
         }
-        const float used = changed ? drifted : target;
-        rem -= used;
-        p.tts -= used;
-        if (rem == 0.f) {// measurement boundary (modelSimulator.cpp:182-188)
-            const std::uint32_t next = P.step + 1U;
-            out.boundary = true;
-            if (next >= P.n_steps) { return out; }
-            out.alive = true;
-            if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
-                const int sign = meta_sign(p.meta);
-                out.tallied = true;
-                out.sensor = sensor;
-                out.fx = __float2ll_rn(static_cast<float>(sign) * v * p.dx * kFluxScale);
-                out.fy = __float2ll_rn(static_cast<float>(sign) * v * p.dy * kFluxScale);
+    }
+    const float left = L.target - L.drifted;
+    bool event_over = true;
+    if (ebest < 0 || tbest > left) {
+        p.px += wx * left;
+        p.py += wy * left;
+        L.drifted = L.target;
+    } else {
+        p.px += wx * tbest;
+        p.py += wy * tbest;
+        L.drifted += tbest;
+        const float4 E = C->edge[ebest];
+        const int link = C->link[ebest];
+        std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
+        if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
+            const CellF32* N = P.cells32 + link;
+            bool pass = true;
+            if (N->material != L.mat) {
+                const MaterialDev& mt = P.materials[N->material];
+                const float w = omega32(P, p.binw, phasor);
+                pass = !(w > (meta_pol(p.meta) == 0 ? mt.w_max_la : mt.w_max_ta));
             }
-            return out;
-        }
-        if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
-            const float3 r = rates32(P.materials[mat], P.sensors[sensor], omega32(P, p.binw, phasor), pol);
-            const float sum = r.x + r.y + r.z;
-            const float u = rs.uf();
-            if (u <= (r.x + r.y) / sum) {
-                sample_freq(P, p, rs, P.sensors[sensor].scatter_table, mat);
-                pol = meta_pol(p.meta);
-                v = vel32(P, p.binw, pol, phasor);
-                if (u > r.x / sum) {
-                    iso_dir(p, rs);
-                    p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
+            if (pass) {
+                p.px += C->offset[ebest].x;
+                p.py += C->offset[ebest].y;
+                entry_next = (C->rev >> (2 * ebest)) & 3U;
+                cell = static_cast<std::uint32_t>(link);
+                C = N;
+                if (C->sensor != L.sensor) {
+                    L.sensor = C->sensor;
+                    L.changed = true;
                 }
-            } else if (r.z > 0.f) {
+                L.mat = C->material;
+            } else {
+                const float flip = ((C->rev >> (8 + ebest)) & 1U) ? -1.f : 1.f;
+                diffuse_dir(p, rs, -E.x * flip, -E.y * flip);
+            }
+        } else if (link == -1) {
+            reflect(p, rs, C->spec, E);
+        } else {// EmitSurface::handlePhonon (psim/src/surface.cpp:61-65)
+            const EmitterDev& em = P.emitters[static_cast<std::uint32_t>(-(link + 2))];
+            if (P.step >= em.absorb_lo && P.step <= em.absorb_hi) {
+                out = Outcome{ false, false, false, 0U, 0, 0 };
+                return true;// absorbed
+            }
+            reflect(p, rs, C->spec, E);
+        }
+        p.meta = meta_with_cell_edge(p.meta, cell, entry_next);
+        if (++L.ncoll > kMaxCollisions) {// stuck in a corner: random point in the cell
+            float r1 = rs.uf();
+            float r2 = rs.uf();
+            if (r1 + r2 > 1.f) {
+                r1 = 1.f - r1;
+                r2 = 1.f - r2;
+            }
+            p.px = C->vert[1].x * r1 + C->vert[2].x * r2;
+            p.py = C->vert[1].y * r1 + C->vert[2].y * r2;
+            p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
+            L.drifted = L.target;
+            ++relocations;
+        } else {
+            event_over = L.changed;
+        }
+    }
+    if (!event_over) { return false; }
+    // The event: measurement boundary, scattering, or a new sensor area (modelSimulator.cpp:178-193)
+    const float used = L.changed ? L.drifted : L.target;
+    L.rem -= used;
+    p.tts -= used;
+    L.need_target = true;
+    if (L.rem == 0.f) {
+        const std::uint32_t next = P.step + 1U;
+        out = Outcome{ false, true, false, 0U, 0, 0 };
+        if (next >= P.n_steps) { return true; }
+        out.alive = true;
+        if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
+            const float sv = static_cast<float>(meta_sign(p.meta)) * L.v;
+            out.tallied = true;
+            out.sensor = L.sensor;
+            out.fx = __float2ll_rn(sv * p.dx * kFluxScale);
+            out.fy = __float2ll_rn(sv * p.dy * kFluxScale);
+        }
+        return true;
+    }
+    if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
+        const int pol = meta_pol(p.meta);
+        const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), pol);
+        const float sum = r.x + r.y + r.z;
+        const float u = rs.uf();
+        if (u <= (r.x + r.y) / sum) {
+            sample_freq(P, p, rs, P.sensors[L.sensor].scatter_table, L.mat);
+            L.v = vel32(P, p.binw, meta_pol(p.meta), phasor);
+            if (u > r.x / sum) {
                 iso_dir(p, rs);
                 p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
             }
-        } else {
-            p.tts = 0.f;// new sensor area (or phasor): draw a fresh scattering time
+        } else if (r.z > 0.f) {
+            iso_dir(p, rs);
+            p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
         }
+    } else {
+        p.tts = 0.f;// new sensor area (or phasor): draw a fresh scattering time
     }
+    return false;
 }
 
-__global__ void __launch_bounds__(kBlock) step_kernel_f32(const StepParams P) {
+// Persistent lanes: each lane pulls the next phonon of the step (alive phonons first, then the
+// step's newborns) from a warp-aggregated work counter and advances it one segment per
+// iteration; a lane whose phonon finishes the step writes it out and takes the next one.  The
+// warp stays full until the step's work runs out instead of waiting for its slowest phonon.
+__global__ void __launch_bounds__(kBlock, 4) step_kernel_f32(const StepParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     BlockTally bt;
     tally_init(P, bt, smem);
     const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *P.count_clear = 0U;
+        *P.work_clear = 0U;
         atomicMax(P.counters + 3, static_cast<unsigned long long>(n_alive) + P.n_new);
+        if (P.population != nullptr) { P.population[P.step] = n_alive + P.n_new; }
     }
     const std::uint32_t total = n_alive + P.n_new;
     const std::uint32_t slot_k = P.step + 1U >= P.step_adj ? P.step + 1U - P.step_adj : 0U;
@@ -305,35 +351,47 @@ __global__ void __launch_bounds__(kBlock) step_kernel_f32(const StepParams P) {
     const uint4* in_meta = reinterpret_cast<const uint4*>(in_pd + P.capacity);
     float4* out_pd = static_cast<float4*>(P.out);
     uint4* out_meta = reinterpret_cast<uint4*>(out_pd + P.capacity);
+    const unsigned full = 0xFFFFFFFFU;
+    const unsigned lane_id = threadIdx.x & 31U;
+    const unsigned below = (1U << lane_id) - 1U;
     unsigned long long steps = 0;
     unsigned long long relocations = 0;
     unsigned long long limits = 0;
-    const std::uint32_t stride = gridDim.x * blockDim.x;
-    for (std::uint32_t base = blockIdx.x * blockDim.x; base < total; base += stride) {
-        const std::uint32_t i = base + threadIdx.x;
-        Outcome o{ false, false, false, 0U, 0, 0 };
-        Ph32 p{ 0.f, 0.f, 0.f, 0.f, 0U, 0U, 0.f, 0U };
-        if (i < total) {
-            Stream rs;
-            float rem;
-            if (i < n_alive) {
-                const float4 a = in_pd[i];
-                const uint4 b = in_meta[i];
-                p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
-                rs.init(P.key0, P.key1, P.step, p.id);
-                rem = P.dt;
-            } else {
-                rem = spawn32(P, p, rs, i - n_alive);
+    bool active = false;
+    bool exhausted = false;// warp-uniform: the step's work counter has run out
+    Lane L;
+    L.p = Ph32{ 0.f, 0.f, 0.f, 0.f, 0U, 0U, 0.f, 0U };
+    while (true) {
+        if (!exhausted) {
+            const unsigned need = __ballot_sync(full, !active);
+            if (need != 0U) {
+                const int leader = __ffs(static_cast<int>(need)) - 1;
+                std::uint32_t base = 0;
+                if (static_cast<int>(lane_id) == leader) { base = atomicAdd(P.work, static_cast<std::uint32_t>(__popc(need))); }
+                base = __shfl_sync(full, base, leader);
+                if (base + static_cast<std::uint32_t>(__popc(need)) >= total) { exhausted = true; }
+                if (!active) {
+                    const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & below));
+                    if (i < total) {
+                        lane_start(P, L, i, n_alive, in_pd, in_meta);
+                        active = true;
+                    }
+                }
             }
-            o = transport32(P, p, rs, rem, relocations, limits);
-            steps += o.boundary ? 1ULL : 0ULL;
         }
-        const std::uint32_t slot = reserve_slot(P, o.alive);
+        if (__ballot_sync(full, active) == 0U) { break; }
+        Outcome o{ false, false, false, 0U, 0, 0 };
+        bool done = false;
+        if (active) { done = segment32(P, L, o, relocations, limits); }
+        const bool finishing = active && done;
+        steps += (finishing && o.boundary) ? 1ULL : 0ULL;
+        const std::uint32_t slot = reserve_slot(P, finishing && o.alive);
         if (slot != 0xFFFFFFFFU) {
-            out_pd[slot] = make_float4(p.px, p.py, p.dx, p.dy);
-            out_meta[slot] = make_uint4(p.meta, p.binw, __float_as_uint(p.tts), p.id);
+            out_pd[slot] = make_float4(L.p.px, L.p.py, L.p.dx, L.p.dy);
+            out_meta[slot] = make_uint4(L.p.meta, L.p.binw, __float_as_uint(L.p.tts), L.p.id);
         }
-        tally_add(P, bt, o.tallied, o.sensor, meta_sign(p.meta), o.fx, o.fy, slot_k);
+        tally_add(P, bt, finishing && o.tallied, o.sensor, meta_sign(L.p.meta), o.fx, o.fy, slot_k);
+        if (finishing) { active = false; }
     }
     block_count_add(P.counters + 0, steps);
     block_count_add(P.counters + 1, relocations);

@@ -292,6 +292,7 @@ __global__ void __launch_bounds__(kBlock) step_kernel_f64(const StepParams P) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *P.count_clear = 0U;
         atomicMax(P.counters + 3, static_cast<unsigned long long>(n_alive) + P.n_new);
+        if (P.population != nullptr) { P.population[P.step] = n_alive + P.n_new; }
     }
     const std::uint32_t total = n_alive + P.n_new;
     const std::uint32_t slot_k = P.step + 1U >= P.step_adj ? P.step + 1U - P.step_adj : 0U;
