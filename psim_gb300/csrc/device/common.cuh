@@ -238,6 +238,11 @@ struct StepParams {
     std::uint32_t* work;              // this step's work counter (phonons handed to lanes)
     std::uint32_t* work_clear;        // the counter of two steps ahead, cleared by this step
     std::uint32_t* population;        // [n_steps] phonons in flight per step (may be null)
+    // Shared-memory staging of read-only tables (FP32 kernel): bit 0 cells, 1 alias tables,
+    // 2 velocities + bin centres; byte offsets of each staged segment and of the tallies.
+    std::uint32_t stage_mask;
+    std::uint32_t off_cells, off_alias, off_vel, off_centre, off_tally;
+    std::uint32_t n_cells, n_tables, n_materials;
     // step
     std::uint32_t step;               // 0-based step index; phonons alive at its end reach boundary step+1
     std::uint32_t n_steps;
@@ -250,7 +255,7 @@ struct StepParams {
     std::uint32_t key0, key1;
     TallySlot* tally;                 // [n_recorded][n_sensors]
     unsigned long long* counters;     // [0] phonon-steps, [1] collision-limit relocations, [2] overflow,
-                                      // [3] max population, [4] event-limit hits
+                                      // [3] max population, [4] event-limit hits, [5] staging timeouts
 };
 
 }// namespace psim::gpu

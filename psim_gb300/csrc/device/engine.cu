@@ -16,13 +16,14 @@
 #include "../host/geom64.hpp"
 #include "cells.hpp"
 #include "common.cuh"
+#include "transport.cuh"
 
 namespace psim::gpu {
 
-void launch_step_f32(const StepParams& P, int grid, cudaStream_t stream);
-void launch_step_f64(const StepParams& P, int grid, cudaStream_t stream);
-int occupancy_f32();
-int occupancy_f64();
+void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
+void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
+int occupancy_f32(int block, std::size_t smem);
+int occupancy_f64(std::size_t smem);
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
                       double* stats_h, cudaStream_t stream);
 void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream);
@@ -546,8 +547,62 @@ void Engine::run(int precision, void* stream_ptr) {
     P.counters = I.counters.as<unsigned long long>();
     P.population = I.population.as<std::uint32_t>();
     auto* counts = I.counts.as<std::uint32_t>();
-    const int occ = std::max(1, fp64 ? occupancy_f64() : occupancy_f32());
+    // Launch shape and shared memory.  The FP32 kernel stages the cell records and the
+    // alias / velocity / bin-centre tables into shared memory (TMA bulk copies) when they fit
+    // next to the block's tally, and then runs one 1024-thread block per SM.
+    const std::size_t tally_b = tally_smem_bytes(d.n_sensors);
+    P.n_cells = d.n_cells;
+    P.n_tables = d.n_tables;
+    P.n_materials = d.n_materials;
+    P.stage_mask = 0U;
+    P.off_tally = 0U;
+    std::size_t smem = tally_b;
+    int block = 256;
+    bool stage = stage_tables_;
+    if (const char* st = std::getenv("PSIM_GB300_STAGE"); st != nullptr && std::atoi(st) == 0) { stage = false; }
+    if (!fp64 && stage) {
+        int dev = 0;
+        int optin = 0;
+        check(cudaGetDevice(&dev), "cudaGetDevice");
+        check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device attribute");
+        const std::size_t budget = static_cast<std::size_t>(optin) - 1024;// static shared memory and slack
+        const std::size_t cells_b = static_cast<std::size_t>(d.n_cells) * sizeof(CellF32);
+        const std::size_t alias_b = static_cast<std::size_t>(d.n_tables) * kAliasCols * 4;
+        const std::size_t vel_b = static_cast<std::size_t>(d.n_materials) * 2 * kBins * 4;
+        const std::size_t centre_b = static_cast<std::size_t>(d.n_materials) * kBins * 4;
+        std::size_t used = 0;
+        auto take = [&](std::size_t bytes, std::uint32_t bit, std::uint32_t* off) {
+            if (used + bytes + tally_b <= budget) {
+                *off = static_cast<std::uint32_t>(used);
+                used += bytes;
+                P.stage_mask |= bit;
+            }
+        };
+        take(cells_b, 1U, &P.off_cells);
+        take(alias_b, 2U, &P.off_alias);
+        if (used + vel_b + centre_b + tally_b <= budget) {
+            P.off_vel = static_cast<std::uint32_t>(used);
+            P.off_centre = static_cast<std::uint32_t>(used + vel_b);
+            used += vel_b + centre_b;
+            P.stage_mask |= 4U;
+        }
+        if (P.stage_mask != 0U) {
+            P.off_tally = static_cast<std::uint32_t>(used);
+            smem = used + tally_b;
+            block = 1024;
+        }
+    }
+    int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(block, smem);
+    if (occ <= 0 && !fp64 && P.stage_mask != 0U) {// cannot launch staged: fall back to global tables
+        P.stage_mask = 0U;
+        P.off_tally = 0U;
+        smem = tally_b;
+        block = 256;
+        occ = occupancy_f32(block, smem);
+    }
+    occ = std::max(1, occ);
     int grid = grid_override_ > 0 ? grid_override_ : I.sms * occ;
+    last_stage_mask_ = P.stage_mask;
     if (const char* g = std::getenv("PSIM_GB300_GRID"); g != nullptr && std::atoi(g) > 0) { grid = std::atoi(g); }// launch-shape override
 
     auto enqueue = [&]() {
@@ -565,9 +620,9 @@ void Engine::run(int precision, void* stream_ptr) {
             P.n_new = I.n_new[s];
             P.id_base = I.id_base[s];
             if (fp64) {
-                launch_step_f64(P, grid, stream);
+                launch_step_f64(P, grid, smem, stream);
             } else {
-                launch_step_f32(P, grid, stream);
+                launch_step_f32(P, grid, block, smem, stream);
             }
         }
     };
@@ -598,6 +653,7 @@ void Engine::run(int precision, void* stream_ptr) {
     counters_.phonon_steps += c[0];
     counters_.relocations += c[1];
     counters_.event_limits += c[4];
+    if (c[5] != 0) { throw std::runtime_error("CUDA staging of the model tables into shared memory timed out"); }
     counters_.overflow += c[2];
     counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
     counters_.kernel_ms += ms;

@@ -85,6 +85,9 @@ public:
     void set_step_adjustment(std::uint64_t adj) { desc_.step_adj = adj; }
     void set_use_graph(bool on) { use_graph_ = on; }
     void set_grid(int blocks) { grid_override_ = blocks; }
+    // Stage cells and tables into shared memory in the FP32 kernel when they fit (default on).
+    void set_stage_tables(bool on) { stage_tables_ = on; }
+    std::uint32_t last_stage_mask() const noexcept { return last_stage_mask_; }
 
     // Phonons in flight at each measurement step of the last run (alive + born), [steps].
     void population(std::uint32_t* out) const;
@@ -109,6 +112,8 @@ private:
     mutable RunCounters counters_;
     std::uint64_t model_bytes_{ 0 };
     bool use_graph_{ true };
+    bool stage_tables_{ true };
+    std::uint32_t last_stage_mask_{ 0 };
     int grid_override_{ 0 };
 };
 

@@ -19,6 +19,22 @@
 namespace psim::gpu {
 namespace {
 
+extern __shared__ __align__(16) unsigned char g_smem[];
+
+// Read-only tables: the shared-memory copy when the host staged it, else global memory.
+__device__ __forceinline__ const CellF32* cells_of(const StepParams& P) {
+    return (P.stage_mask & 1U) ? reinterpret_cast<const CellF32*>(g_smem + P.off_cells) : cells_of(P);
+}
+__device__ __forceinline__ const std::uint32_t* alias_of(const StepParams& P) {
+    return (P.stage_mask & 2U) ? reinterpret_cast<const std::uint32_t*>(g_smem + P.off_alias) : P.alias;
+}
+__device__ __forceinline__ const float* vel_of(const StepParams& P) {
+    return (P.stage_mask & 4U) ? reinterpret_cast<const float*>(g_smem + P.off_vel) : P.vel32;
+}
+__device__ __forceinline__ const float* centre_of(const StepParams& P) {
+    return (P.stage_mask & 4U) ? reinterpret_cast<const float*>(g_smem + P.off_centre) : P.centre32;
+}
+
 struct Ph32 {
     float px, py, dx, dy;
     std::uint32_t meta, binw;
@@ -28,8 +44,7 @@ struct Ph32 {
 
 // Group velocity of the phonon's bin (Material::getVel, psim/src/material.cpp:82-84).
 __device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
-    return phasor ? 1000.f
-                  : __ldg(P.vel32 + (smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw));
+    return phasor ? 1000.f : vel_of(P)[(smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw)];
 }
 
 // Frequency in units of 1e13 rad/s (Material::getFreq, psim/src/material.cpp:77-80): bin
@@ -37,7 +52,7 @@ __device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, 
 __device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
     if (phasor) { return 1e-13f; }
     const std::uint32_t sm = smat_of(binw);
-    const float c = __ldg(P.centre32 + sm * kBins + bin_of(binw));
+    const float c = centre_of(P)[sm * kBins + bin_of(binw)];
     if (P.full_sim) { return c; }
     const float u = (static_cast<float>(jitter_of(binw)) + 0.5f) * (1.0f / 262144.0f);
     return c + (2.f * u - 1.f) * (P.materials[sm].width * 0.5f);
@@ -54,7 +69,12 @@ __device__ __forceinline__ float3 rates32(const MaterialDev& m, const SensorDev&
         u = n;
     } else {
         n = (w < m.w_cut) ? m.cTN * w * s.T4 : 0.f;
-        u = (w >= m.w_cut) ? m.cTU * w2 / sinhf(w * s.xk) : 0.f;
+        if (w >= m.w_cut) {// sinh(x) = (e^x - e^-x) / 2 with x = hbar w / kT, here x > 0.1
+            const float ex = __expf(w * s.xk);
+            u = m.cTU * w2 / (0.5f * (ex - 1.f / ex));
+        } else {
+            u = 0.f;
+        }
     }
     return make_float3(n, u, m.cI * w2 * w2);
 }
@@ -90,7 +110,7 @@ __device__ __forceinline__ void reflect(Ph32& p, Stream& rs, float spec, float4 
 // material 'mat'.
 __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
                                             std::uint32_t mat) {
-    const std::uint32_t o = alias_draw(P.alias + static_cast<std::size_t>(table) * kAliasCols, rs.next());
+    const std::uint32_t o = alias_draw(alias_of(P) + static_cast<std::size_t>(table) * kAliasCols, rs.next());
     const std::uint32_t jit = P.full_sim ? 0U : (rs.next() >> 14);
     p.binw = make_binw(o >> 1, mat, jit);
     p.meta = meta_with_pol(p.meta, static_cast<int>(o & 1U));
@@ -105,7 +125,7 @@ __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& r
     p.tts = 0.f;
     if (g.source >= 0) {
         const std::uint32_t cell = static_cast<std::uint32_t>(g.source);
-        const CellF32& c = P.cells32[cell];
+        const CellF32& c = cells_of(P)[cell];
         p.meta = make_meta(cell, kNoEdge, 0, g.sign, false);
         sample_freq(P, p, rs, P.sensors[c.sensor].base_table, c.material);
         float r1 = rs.uf();
@@ -123,7 +143,7 @@ __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& r
     const float t_birth = g.t0 + g.span * rs.uf();
     const bool phasor = P.phasor_sim != 0;
     p.meta = make_meta(e.cell, e.edge, 0, g.sign, phasor);
-    sample_freq(P, p, rs, e.table, P.cells32[e.cell].material);
+    sample_freq(P, p, rs, e.table, cells_of(P)[e.cell].material);
     const float r = rs.uf();
     p.px = e.a.x * r + e.b.x * (1.f - r);
     p.py = e.a.y * r + e.b.y * (1.f - r);
@@ -151,7 +171,8 @@ struct Lane {
     std::uint32_t sensor, mat;
     int ncoll;      // impacts in the current event (MAX_COLLISIONS rule)
     unsigned events;
-    bool need_target, changed;
+    float fN, fNU;  // N/sum and (N+U)/sum of the rates of the last scattering-time draw
+    bool need_target, changed, rates_ok;
 };
 
 struct Outcome {
@@ -173,11 +194,12 @@ __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::ui
     } else {
         L.rem = spawn32(P, L.p, L.rs, i - n_alive);
     }
-    const CellF32* C = P.cells32 + meta_cell(L.p.meta);
+    const CellF32* C = cells_of(P) + meta_cell(L.p.meta);
     L.sensor = C->sensor;
     L.mat = C->material;
     L.v = vel32(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
     L.need_target = true;
+    L.rates_ok = false;
     L.events = 0;
 }
 
@@ -198,7 +220,11 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         }
         if (p.tts <= 0.f) {// time to the next scattering event (modelSimulator.cpp:148-153)
             const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), meta_pol(p.meta));
-            p.tts = 1e9f * (-__logf(rs.uf())) / (r.x + r.y + r.z);
+            const float sum = r.x + r.y + r.z;
+            p.tts = 1e9f * (-__logf(rs.uf())) / sum;
+            L.fN = r.x / sum;
+            L.fNU = (r.x + r.y) / sum;
+            L.rates_ok = true;
         }
         L.target = (L.rem <= p.tts) ? L.rem : p.tts;
         L.drifted = 0.f;
@@ -207,7 +233,7 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         L.need_target = false;
     }
     std::uint32_t cell = meta_cell(p.meta);
-    const CellF32* C = P.cells32 + cell;
+    const CellF32* C = cells_of(P) + cell;
     const float wx = p.dx * L.v;
     const float wy = p.dy * L.v;
     const std::uint32_t entry = meta_edge(p.meta);
@@ -239,7 +265,7 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         const int link = C->link[ebest];
         std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
         if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
-            const CellF32* N = P.cells32 + link;
+            const CellF32* N = cells_of(P) + link;
             bool pass = true;
             if (N->material != L.mat) {
                 const MaterialDev& mt = P.materials[N->material];
@@ -309,21 +335,25 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         return true;
     }
     if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
-        const int pol = meta_pol(p.meta);
-        const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), pol);
-        const float sum = r.x + r.y + r.z;
+        if (!L.rates_ok) {// the scattering time was drawn in an earlier step: recompute its rates
+            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), meta_pol(p.meta));
+            const float sum = r.x + r.y + r.z;
+            L.fN = r.x / sum;
+            L.fNU = (r.x + r.y) / sum;
+        }
         const float u = rs.uf();
-        if (u <= (r.x + r.y) / sum) {
+        if (u <= L.fNU) {// normal or Umklapp: resample frequency, velocity and polarization
             sample_freq(P, p, rs, P.sensors[L.sensor].scatter_table, L.mat);
             L.v = vel32(P, p.binw, meta_pol(p.meta), phasor);
-            if (u > r.x / sum) {
+            if (u > L.fN) {// Umklapp: also a new direction
                 iso_dir(p, rs);
                 p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
             }
-        } else if (r.z > 0.f) {
+        } else if (L.fNU < 1.f) {// impurity (its rate is positive): new direction only
             iso_dir(p, rs);
             p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
         }
+        L.rates_ok = false;
     } else {
         p.tts = 0.f;// new sensor area (or phasor): draw a fresh scattering time
     }
@@ -334,10 +364,35 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
 // step's newborns) from a warp-aggregated work counter and advances it one segment per
 // iteration; a lane whose phonon finishes the step writes it out and takes the next one.  The
 // warp stays full until the step's work runs out instead of waiting for its slowest phonon.
-__global__ void __launch_bounds__(kBlock, 4) step_kernel_f32(const StepParams P) {
-    extern __shared__ __align__(16) unsigned char smem[];
+__global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
+    __shared__ std::uint64_t stage_bar;
+    if (P.stage_mask != 0U) {// TMA bulk copies of the read-only tables into shared memory
+        if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned cells_b = (P.stage_mask & 1U) ? P.n_cells * static_cast<unsigned>(sizeof(CellF32)) : 0U;
+            const unsigned alias_b = (P.stage_mask & 2U) ? P.n_tables * kAliasCols * 4U : 0U;
+            const unsigned vel_b = (P.stage_mask & 4U) ? P.n_materials * 2U * kBins * 4U : 0U;
+            const unsigned centre_b = (P.stage_mask & 4U) ? P.n_materials * kBins * 4U : 0U;
+            mbar_expect_tx(&stage_bar, cells_b + alias_b + vel_b + centre_b);
+            if (cells_b != 0U) { bulk_to_shared(g_smem + P.off_cells, P.cells32, cells_b, &stage_bar); }
+            if (alias_b != 0U) { bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, &stage_bar); }
+            if (vel_b != 0U) {
+                bulk_to_shared(g_smem + P.off_vel, P.vel32, vel_b, &stage_bar);
+                bulk_to_shared(g_smem + P.off_centre, P.centre32, centre_b, &stage_bar);
+            }
+        }
+    }
     BlockTally bt;
-    tally_init(P, bt, smem);
+    tally_init(P, bt, g_smem);
+    if (P.stage_mask != 0U) {
+        const bool ok = mbar_wait_bounded(&stage_bar);
+        if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
+            if (threadIdx.x == 0) { atomicAdd(P.counters + 5, 1ULL); }
+            mbar_wait_bounded(&stage_bar);
+            return;
+        }
+    }
     const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *P.count_clear = 0U;
@@ -401,15 +456,21 @@ __global__ void __launch_bounds__(kBlock, 4) step_kernel_f32(const StepParams P)
 
 }// namespace
 
-void launch_step_f32(const StepParams& P, int grid, cudaStream_t stream) {
-    step_kernel_f32<<<grid, kBlock, kTallySmem, stream>>>(P);
+void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
+    step_kernel_f32<<<grid, block, smem, stream>>>(P);
 }
 
-int occupancy_f32() {
+int occupancy_f32(int block, std::size_t smem) {
+    if (smem > 48 * 1024) {
+        if (cudaFuncSetAttribute(step_kernel_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+    }
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f32, kBlock, kTallySmem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f32, block, smem) != cudaSuccess) {
         cudaGetLastError();
-        return 1;
+        return 0;
     }
     return blocks;
 }

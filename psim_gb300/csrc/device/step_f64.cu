@@ -346,13 +346,13 @@ __global__ void __launch_bounds__(kBlock) step_kernel_f64(const StepParams P) {
 
 }// namespace
 
-void launch_step_f64(const StepParams& P, int grid, cudaStream_t stream) {
-    step_kernel_f64<<<grid, kBlock, kTallySmem, stream>>>(P);
+void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream) {
+    step_kernel_f64<<<grid, kBlock, smem, stream>>>(P);
 }
 
-int occupancy_f64() {
+int occupancy_f64(std::size_t smem) {
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f64, kBlock, kTallySmem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f64, kBlock, smem) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }

@@ -14,7 +14,7 @@ constexpr int kSharedSensors = 2048;   // sensors tallied in shared memory; larg
 // column (top 11 bits) and decides acceptance (low 21 bits).
 __device__ __forceinline__ std::uint32_t alias_draw(const std::uint32_t* table, std::uint32_t x) {
     const std::uint32_t col = x >> 21;
-    const std::uint32_t e = __ldg(table + col);
+    const std::uint32_t e = table[col];
     const std::uint32_t o = ((x & 0x1FFFFFU) < (e >> 11)) ? col : (e & 0x7FFU);
     return min(o, static_cast<std::uint32_t>(2 * kBins - 1));// columns >= 2000 carry no probability
 }
@@ -63,6 +63,45 @@ __device__ __forceinline__ void tally_add(const StepParams& P, BlockTally& bt, b
     }
 }
 
+// ---------------------------------------------------------------- TMA bulk copies into shared memory
+__device__ __forceinline__ std::uint32_t smem_u32(const void* p) { return static_cast<std::uint32_t>(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(std::uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(std::uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// One 1-D bulk copy global -> shared by the TMA engine, completing on the mbarrier.
+// Both addresses must be 16-byte aligned and the size a multiple of 16.
+__device__ __forceinline__ void bulk_to_shared(void* dst, const void* src, unsigned bytes, std::uint64_t* bar) {
+    std::uint64_t gsrc;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+                 "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0U;
+}
+
+// Bounded wait for phase 0 of the staging barrier; false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar) {
+    for (unsigned it = 0; it < (1U << 22); ++it) {
+        if (mbar_try_wait(bar, 0U)) { return true; }
+    }
+    return false;
+}
+
 __device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt, std::uint32_t slot) {
     if (!bt.shared) { return; }
     __syncthreads();
@@ -80,10 +119,11 @@ __device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt,
 }
 
 __device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, unsigned char* smem) {
+    // layout: fx[S], fy[S] (8-byte aligned), count[S]; S <= kSharedSensors
     bt.shared = P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors);
-    bt.fx = reinterpret_cast<long long*>(smem);
-    bt.fy = bt.fx + kSharedSensors;
-    bt.count = reinterpret_cast<int*>(bt.fy + kSharedSensors);
+    bt.fx = reinterpret_cast<long long*>(smem + P.off_tally);
+    bt.fy = bt.fx + P.n_sensors;
+    bt.count = reinterpret_cast<int*>(bt.fy + P.n_sensors);
     if (bt.shared) {
         for (std::uint32_t s = threadIdx.x; s < P.n_sensors; s += blockDim.x) {
             bt.fx[s] = 0;
@@ -94,7 +134,10 @@ __device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, 
     __syncthreads();
 }
 
-constexpr std::size_t kTallySmem = kSharedSensors * (2 * sizeof(long long) + sizeof(int));
+// Shared bytes of a block's tally for S sensors (0 when S exceeds kSharedSensors), 16-aligned.
+inline std::size_t tally_smem_bytes(std::uint32_t S) {
+    return S <= static_cast<std::uint32_t>(kSharedSensors) ? ((static_cast<std::size_t>(S) * 20 + 15) / 16) * 16 : 0;
+}
 
 // Warp-aggregated slot reservation in the output buffer; returns the slot or UINT32_MAX.
 __device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool alive) {

@@ -46,6 +46,13 @@ def test_launch_shape_does_not_change_results(api, monkeypatch):
         m2.run(seed=9)
         got = m2.tallies()
         assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1]), grid
+    monkeypatch.delenv("PSIM_GB300_GRID")
+    # tables read from global memory instead of the shared-memory copies
+    monkeypatch.setenv("PSIM_GB300_STAGE", "0")
+    m3 = api.Model(model_path("bar_ss"))
+    m3.run(seed=9)
+    got = m3.tallies()
+    assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
 
 
 def test_counters_and_phonon_steps(api):
