@@ -22,7 +22,7 @@ namespace psim::gpu {
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
-int occupancy_f32(int block, std::size_t smem);
+int occupancy_f32(bool staged, int block, std::size_t smem);
 int occupancy_f64(std::size_t smem);
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
                       double* stats_h, cudaStream_t stream);
@@ -570,35 +570,25 @@ void Engine::run(int precision, void* stream_ptr) {
         const std::size_t alias_b = static_cast<std::size_t>(d.n_tables) * kAliasCols * 4;
         const std::size_t vel_b = static_cast<std::size_t>(d.n_materials) * 2 * kBins * 4;
         const std::size_t centre_b = static_cast<std::size_t>(d.n_materials) * kBins * 4;
-        std::size_t used = 0;
-        auto take = [&](std::size_t bytes, std::uint32_t bit, std::uint32_t* off) {
-            if (used + bytes + tally_b <= budget) {
-                *off = static_cast<std::uint32_t>(used);
-                used += bytes;
-                P.stage_mask |= bit;
-            }
-        };
-        take(cells_b, 1U, &P.off_cells);
-        take(alias_b, 2U, &P.off_alias);
-        if (used + vel_b + centre_b + tally_b <= budget) {
-            P.off_vel = static_cast<std::uint32_t>(used);
-            P.off_centre = static_cast<std::uint32_t>(used + vel_b);
-            used += vel_b + centre_b;
-            P.stage_mask |= 4U;
-        }
-        if (P.stage_mask != 0U) {
+        const std::size_t used = cells_b + alias_b + vel_b + centre_b;
+        if (used + tally_b <= budget) {// everything or nothing: the staged kernel reads every table from shared memory
+            P.off_cells = 0U;
+            P.off_alias = static_cast<std::uint32_t>(cells_b);
+            P.off_vel = static_cast<std::uint32_t>(cells_b + alias_b);
+            P.off_centre = static_cast<std::uint32_t>(cells_b + alias_b + vel_b);
             P.off_tally = static_cast<std::uint32_t>(used);
+            P.stage_mask = 7U;
             smem = used + tally_b;
             block = 1024;
         }
     }
-    int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(block, smem);
+    int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(P.stage_mask != 0U, block, smem);
     if (occ <= 0 && !fp64 && P.stage_mask != 0U) {// cannot launch staged: fall back to global tables
         P.stage_mask = 0U;
         P.off_tally = 0U;
         smem = tally_b;
         block = 256;
-        occ = occupancy_f32(block, smem);
+        occ = occupancy_f32(false, block, smem);
     }
     occ = std::max(1, occ);
     int grid = grid_override_ > 0 ? grid_override_ : I.sms * occ;

@@ -21,18 +21,35 @@ namespace {
 
 extern __shared__ __align__(16) unsigned char g_smem[];
 
-// Read-only tables: the shared-memory copy when the host staged it, else global memory.
-__device__ __forceinline__ const CellF32* cells_of(const StepParams& P) {
-    return (P.stage_mask & 1U) ? reinterpret_cast<const CellF32*>(g_smem + P.off_cells) : cells_of(P);
+// Read-only tables: the shared-memory copies in the staged kernel (kStaged), else global memory.
+// Compiled as two kernels so each reads its tables with direct shared or global loads.
+template<bool kStaged> __device__ __forceinline__ const CellF32* cells_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const CellF32*>(g_smem + P.off_cells);
+    } else {
+        return P.cells32;
+    }
 }
-__device__ __forceinline__ const std::uint32_t* alias_of(const StepParams& P) {
-    return (P.stage_mask & 2U) ? reinterpret_cast<const std::uint32_t*>(g_smem + P.off_alias) : P.alias;
+template<bool kStaged> __device__ __forceinline__ const std::uint32_t* alias_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const std::uint32_t*>(g_smem + P.off_alias);
+    } else {
+        return P.alias;
+    }
 }
-__device__ __forceinline__ const float* vel_of(const StepParams& P) {
-    return (P.stage_mask & 4U) ? reinterpret_cast<const float*>(g_smem + P.off_vel) : P.vel32;
+template<bool kStaged> __device__ __forceinline__ const float* vel_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const float*>(g_smem + P.off_vel);
+    } else {
+        return P.vel32;
+    }
 }
-__device__ __forceinline__ const float* centre_of(const StepParams& P) {
-    return (P.stage_mask & 4U) ? reinterpret_cast<const float*>(g_smem + P.off_centre) : P.centre32;
+template<bool kStaged> __device__ __forceinline__ const float* centre_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const float*>(g_smem + P.off_centre);
+    } else {
+        return P.centre32;
+    }
 }
 
 struct Ph32 {
@@ -43,16 +60,16 @@ struct Ph32 {
 };
 
 // Group velocity of the phonon's bin (Material::getVel, psim/src/material.cpp:82-84).
-__device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
-    return phasor ? 1000.f : vel_of(P)[(smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw)];
+template<bool S> __device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
+    return phasor ? 1000.f : vel_of<S>(P)[(smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw)];
 }
 
 // Frequency in units of 1e13 rad/s (Material::getFreq, psim/src/material.cpp:77-80): bin
 // centre plus the stored uniform offset inside the bin in a deviational simulation.
-__device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
+template<bool S> __device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
     if (phasor) { return 1e-13f; }
     const std::uint32_t sm = smat_of(binw);
-    const float c = centre_of(P)[sm * kBins + bin_of(binw)];
+    const float c = centre_of<S>(P)[sm * kBins + bin_of(binw)];
     if (P.full_sim) { return c; }
     const float u = (static_cast<float>(jitter_of(binw)) + 0.5f) * (1.0f / 262144.0f);
     return c + (2.f * u - 1.f) * (P.materials[sm].width * 0.5f);
@@ -71,7 +88,7 @@ __device__ __forceinline__ float3 rates32(const MaterialDev& m, const SensorDev&
         n = (w < m.w_cut) ? m.cTN * w * s.T4 : 0.f;
         if (w >= m.w_cut) {// sinh(x) = (e^x - e^-x) / 2 with x = hbar w / kT, here x > 0.1
             const float ex = __expf(w * s.xk);
-            u = m.cTU * w2 / (0.5f * (ex - 1.f / ex));
+            u = __fdividef(2.f * m.cTU * w2 * ex, ex * ex - 1.f);// cTU w^2 / sinh(x)
         } else {
             u = 0.f;
         }
@@ -108,9 +125,9 @@ __device__ __forceinline__ void reflect(Ph32& p, Stream& rs, float spec, float4 
 
 // Material::freqIndex + getFreq (psim/src/material.cpp:64-80) from an alias table of the
 // material 'mat'.
-__device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
+template<bool S> __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
                                             std::uint32_t mat) {
-    const std::uint32_t o = alias_draw(alias_of(P) + static_cast<std::size_t>(table) * kAliasCols, rs.next());
+    const std::uint32_t o = alias_draw(alias_of<S>(P) + static_cast<std::size_t>(table) * kAliasCols, rs.next());
     const std::uint32_t jit = P.full_sim ? 0U : (rs.next() >> 14);
     p.binw = make_binw(o >> 1, mat, jit);
     p.meta = meta_with_pol(p.meta, static_cast<int>(o & 1U));
@@ -118,16 +135,16 @@ __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream
 
 // Create newborn j of this step (CellOriginBuilder / SurfaceOriginBuilder / PhasorBuilder,
 // psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
-__device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
+template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
     const BirthGroup g = P.groups[find_group(P, j)];
     p.id = P.id_base + j;
     rs.init(P.key0, P.key1, P.step, p.id);
     p.tts = 0.f;
     if (g.source >= 0) {
         const std::uint32_t cell = static_cast<std::uint32_t>(g.source);
-        const CellF32& c = cells_of(P)[cell];
+        const CellF32& c = cells_of<S>(P)[cell];
         p.meta = make_meta(cell, kNoEdge, 0, g.sign, false);
-        sample_freq(P, p, rs, P.sensors[c.sensor].base_table, c.material);
+        sample_freq<S>(P, p, rs, P.sensors[c.sensor].base_table, c.material);
         float r1 = rs.uf();
         float r2 = rs.uf();
         if (r1 + r2 > 1.f) {
@@ -143,7 +160,7 @@ __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& r
     const float t_birth = g.t0 + g.span * rs.uf();
     const bool phasor = P.phasor_sim != 0;
     p.meta = make_meta(e.cell, e.edge, 0, g.sign, phasor);
-    sample_freq(P, p, rs, e.table, cells_of(P)[e.cell].material);
+    sample_freq<S>(P, p, rs, e.table, cells_of<S>(P)[e.cell].material);
     const float r = rs.uf();
     p.px = e.a.x * r + e.b.x * (1.f - r);
     p.py = e.a.y * r + e.b.y * (1.f - r);
@@ -183,7 +200,7 @@ struct Outcome {
     long long fx, fy;
 };
 
-__device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive,
+template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive,
                                            const float4* in_pd, const uint4* in_meta) {
     if (i < n_alive) {
         const float4 a = in_pd[i];
@@ -192,12 +209,12 @@ __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::ui
         L.rs.init(P.key0, P.key1, P.step, L.p.id);
         L.rem = P.dt;
     } else {
-        L.rem = spawn32(P, L.p, L.rs, i - n_alive);
+        L.rem = spawn32<S>(P, L.p, L.rs, i - n_alive);
     }
-    const CellF32* C = cells_of(P) + meta_cell(L.p.meta);
+    const CellF32* C = cells_of<S>(P) + meta_cell(L.p.meta);
     L.sensor = C->sensor;
     L.mat = C->material;
-    L.v = vel32(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
+    L.v = vel32<S>(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
     L.need_target = true;
     L.rates_ok = false;
     L.events = 0;
@@ -207,7 +224,7 @@ __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::ui
 // the current event (ModelSimulator::simulatePhonon / handleImpacts / nextImpact,
 // psim/src/modelSimulator.cpp:87-225).  Returns true when the phonon's step is over (it
 // reached the step boundary or was absorbed); the outcome says which.
-__device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out, unsigned long long& relocations,
+template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out, unsigned long long& relocations,
                           unsigned long long& limits) {
     Ph32& p = L.p;
     Stream& rs = L.rs;
@@ -219,11 +236,12 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
             p.tts = fmaxf(p.tts, 0.f);
         }
         if (p.tts <= 0.f) {// time to the next scattering event (modelSimulator.cpp:148-153)
-            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), meta_pol(p.meta));
+            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
             const float sum = r.x + r.y + r.z;
-            p.tts = 1e9f * (-__logf(rs.uf())) / sum;
-            L.fN = r.x / sum;
-            L.fNU = (r.x + r.y) / sum;
+            const float inv = __frcp_rn(r.x + r.y + r.z);
+            p.tts = 1e9f * (-__logf(rs.uf())) * inv;
+            L.fN = r.x * inv;
+            L.fNU = (r.x + r.y) * inv;
             L.rates_ok = true;
         }
         L.target = (L.rem <= p.tts) ? L.rem : p.tts;
@@ -233,7 +251,7 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         L.need_target = false;
     }
     std::uint32_t cell = meta_cell(p.meta);
-    const CellF32* C = cells_of(P) + cell;
+    const CellF32* C = cells_of<S>(P) + cell;
     const float wx = p.dx * L.v;
     const float wy = p.dy * L.v;
     const std::uint32_t entry = meta_edge(p.meta);
@@ -244,7 +262,7 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         const float4 E = C->edge[e];
         const float den = E.x * wx + E.y * wy;
         if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
-            const float t = fmaxf((E.z - (E.x * p.px + E.y * p.py)) / den, 0.f);
+            const float t = fmaxf(__fdividef(E.z - (E.x * p.px + E.y * p.py), den), 0.f);
             if (t < tbest) {
                 tbest = t;
                 ebest = e;
@@ -265,11 +283,11 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
         const int link = C->link[ebest];
         std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
         if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
-            const CellF32* N = cells_of(P) + link;
+            const CellF32* N = cells_of<S>(P) + link;
             bool pass = true;
             if (N->material != L.mat) {
                 const MaterialDev& mt = P.materials[N->material];
-                const float w = omega32(P, p.binw, phasor);
+                const float w = omega32<S>(P, p.binw, phasor);
                 pass = !(w > (meta_pol(p.meta) == 0 ? mt.w_max_la : mt.w_max_ta));
             }
             if (pass) {
@@ -336,15 +354,15 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
     }
     if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
         if (!L.rates_ok) {// the scattering time was drawn in an earlier step: recompute its rates
-            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32(P, p.binw, phasor), meta_pol(p.meta));
-            const float sum = r.x + r.y + r.z;
-            L.fN = r.x / sum;
-            L.fNU = (r.x + r.y) / sum;
+            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
+            const float inv = __frcp_rn(r.x + r.y + r.z);
+            L.fN = r.x * inv;
+            L.fNU = (r.x + r.y) * inv;
         }
         const float u = rs.uf();
         if (u <= L.fNU) {// normal or Umklapp: resample frequency, velocity and polarization
-            sample_freq(P, p, rs, P.sensors[L.sensor].scatter_table, L.mat);
-            L.v = vel32(P, p.binw, meta_pol(p.meta), phasor);
+            sample_freq<S>(P, p, rs, P.sensors[L.sensor].scatter_table, L.mat);
+            L.v = vel32<S>(P, p.binw, meta_pol(p.meta), phasor);
             if (u > L.fN) {// Umklapp: also a new direction
                 iso_dir(p, rs);
                 p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
@@ -364,9 +382,9 @@ __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome&
 // step's newborns) from a warp-aggregated work counter and advances it one segment per
 // iteration; a lane whose phonon finishes the step writes it out and takes the next one.  The
 // warp stays full until the step's work runs out instead of waiting for its slowest phonon.
-__global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
+template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
     __shared__ std::uint64_t stage_bar;
-    if (P.stage_mask != 0U) {// TMA bulk copies of the read-only tables into shared memory
+    if constexpr (S) {// TMA bulk copies of the read-only tables into shared memory
         if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -385,7 +403,7 @@ __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
     }
     BlockTally bt;
     tally_init(P, bt, g_smem);
-    if (P.stage_mask != 0U) {
+    if constexpr (S) {
         const bool ok = mbar_wait_bounded(&stage_bar);
         if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
             if (threadIdx.x == 0) { atomicAdd(P.counters + 5, 1ULL); }
@@ -428,7 +446,7 @@ __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
                 if (!active) {
                     const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & below));
                     if (i < total) {
-                        lane_start(P, L, i, n_alive, in_pd, in_meta);
+                        lane_start<S>(P, L, i, n_alive, in_pd, in_meta);
                         active = true;
                     }
                 }
@@ -437,7 +455,7 @@ __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
         if (__ballot_sync(full, active) == 0U) { break; }
         Outcome o{ false, false, false, 0U, 0, 0 };
         bool done = false;
-        if (active) { done = segment32(P, L, o, relocations, limits); }
+        if (active) { done = segment32<S>(P, L, o, relocations, limits); }
         const bool finishing = active && done;
         steps += (finishing && o.boundary) ? 1ULL : 0ULL;
         const std::uint32_t slot = reserve_slot(P, finishing && o.alive);
@@ -457,18 +475,23 @@ __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
 }// namespace
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
-    step_kernel_f32<<<grid, block, smem, stream>>>(P);
+    if (P.stage_mask != 0U) {
+        step_kernel_f32<true><<<grid, block, smem, stream>>>(P);
+    } else {
+        step_kernel_f32<false><<<grid, block, smem, stream>>>(P);
+    }
 }
 
-int occupancy_f32(int block, std::size_t smem) {
+int occupancy_f32(bool staged, int block, std::size_t smem) {
+    const void* fn = staged ? reinterpret_cast<const void*>(step_kernel_f32<true>) : reinterpret_cast<const void*>(step_kernel_f32<false>);
     if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(step_kernel_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
             cudaGetLastError();
             return 0;
         }
     }
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, step_kernel_f32, block, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
