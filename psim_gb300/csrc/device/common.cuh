@@ -100,6 +100,16 @@ struct Stream {
         block = 0;
         left = 0;
     }
+    // Compute the next block of four words now (used where many lanes start a step together).
+    __device__ __forceinline__ void prefill() {
+        const U4 r = philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
+        b0 = r.x;
+        b1 = r.y;
+        b2 = r.z;
+        b3 = r.w;
+        ++block;
+        left = 4;
+    }
     __device__ __forceinline__ std::uint32_t next() {
         if (left == 0) {
             const U4 r = philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
@@ -190,7 +200,12 @@ struct EmitterDev {
     int sign;               // +1 if hotter than t_eq
     std::uint32_t absorb_lo, absorb_hi; // steps s with s*dt >= start and s*dt + dt <= start + duration
     double spec;
+    double pad;
 };
+// Records staged into shared memory by 1-D bulk copies: sizes must be multiples of 16 bytes.
+static_assert(sizeof(SensorDev) % 16 == 0, "SensorDev size");
+static_assert(sizeof(MaterialDev) % 16 == 0, "MaterialDev size");
+static_assert(sizeof(EmitterDev) % 16 == 0, "EmitterDev size");
 
 // A group of phonons born in one step: all from one cell (step 0) or one emitter.
 struct BirthGroup {
@@ -242,6 +257,7 @@ struct StepParams {
     // 2 velocities + bin centres; byte offsets of each staged segment and of the tallies.
     std::uint32_t stage_mask;
     std::uint32_t off_cells, off_alias, off_vel, off_centre, off_tally;
+    std::uint32_t off_sensors, off_materials, off_emitters, n_emitters;
     std::uint32_t n_cells, n_tables, n_materials;
     // step
     std::uint32_t step;               // 0-based step index; phonons alive at its end reach boundary step+1

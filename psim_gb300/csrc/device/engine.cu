@@ -554,6 +554,7 @@ void Engine::run(int precision, void* stream_ptr) {
     P.n_cells = d.n_cells;
     P.n_tables = d.n_tables;
     P.n_materials = d.n_materials;
+    P.n_emitters = d.n_emitters;
     P.stage_mask = 0U;
     P.off_tally = 0U;
     std::size_t smem = tally_b;
@@ -570,12 +571,18 @@ void Engine::run(int precision, void* stream_ptr) {
         const std::size_t alias_b = static_cast<std::size_t>(d.n_tables) * kAliasCols * 4;
         const std::size_t vel_b = static_cast<std::size_t>(d.n_materials) * 2 * kBins * 4;
         const std::size_t centre_b = static_cast<std::size_t>(d.n_materials) * kBins * 4;
-        const std::size_t used = cells_b + alias_b + vel_b + centre_b;
+        const std::size_t sens_b = static_cast<std::size_t>(d.n_sensors) * sizeof(SensorDev);
+        const std::size_t mat_b = static_cast<std::size_t>(d.n_materials) * sizeof(MaterialDev);
+        const std::size_t emit_b = static_cast<std::size_t>(d.n_emitters) * sizeof(EmitterDev);
+        const std::size_t used = cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b;
         if (used + tally_b <= budget) {// everything or nothing: the staged kernel reads every table from shared memory
             P.off_cells = 0U;
             P.off_alias = static_cast<std::uint32_t>(cells_b);
             P.off_vel = static_cast<std::uint32_t>(cells_b + alias_b);
             P.off_centre = static_cast<std::uint32_t>(cells_b + alias_b + vel_b);
+            P.off_sensors = static_cast<std::uint32_t>(cells_b + alias_b + vel_b + centre_b);
+            P.off_materials = static_cast<std::uint32_t>(P.off_sensors + sens_b);
+            P.off_emitters = static_cast<std::uint32_t>(P.off_materials + mat_b);
             P.off_tally = static_cast<std::uint32_t>(used);
             P.stage_mask = 7U;
             smem = used + tally_b;

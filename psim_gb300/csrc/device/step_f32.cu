@@ -44,6 +44,27 @@ template<bool kStaged> __device__ __forceinline__ const float* vel_of(const Step
         return P.vel32;
     }
 }
+template<bool kStaged> __device__ __forceinline__ const SensorDev* sensors_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const SensorDev*>(g_smem + P.off_sensors);
+    } else {
+        return P.sensors;
+    }
+}
+template<bool kStaged> __device__ __forceinline__ const MaterialDev* materials_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const MaterialDev*>(g_smem + P.off_materials);
+    } else {
+        return P.materials;
+    }
+}
+template<bool kStaged> __device__ __forceinline__ const EmitterDev* emitters_of(const StepParams& P) {
+    if constexpr (kStaged) {
+        return reinterpret_cast<const EmitterDev*>(g_smem + P.off_emitters);
+    } else {
+        return P.emitters;
+    }
+}
 template<bool kStaged> __device__ __forceinline__ const float* centre_of(const StepParams& P) {
     if constexpr (kStaged) {
         return reinterpret_cast<const float*>(g_smem + P.off_centre);
@@ -72,7 +93,7 @@ template<bool S> __device__ __forceinline__ float omega32(const StepParams& P, s
     const float c = centre_of<S>(P)[sm * kBins + bin_of(binw)];
     if (P.full_sim) { return c; }
     const float u = (static_cast<float>(jitter_of(binw)) + 0.5f) * (1.0f / 262144.0f);
-    return c + (2.f * u - 1.f) * (P.materials[sm].width * 0.5f);
+    return c + (2.f * u - 1.f) * (materials_of<S>(P)[sm].width * 0.5f);
 }
 
 // Relaxation rates [N, U, I] (Material::tauNInv/tauUInv/tauIInv, psim/src/material.cpp:207-239),
@@ -144,7 +165,7 @@ template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, P
         const std::uint32_t cell = static_cast<std::uint32_t>(g.source);
         const CellF32& c = cells_of<S>(P)[cell];
         p.meta = make_meta(cell, kNoEdge, 0, g.sign, false);
-        sample_freq<S>(P, p, rs, P.sensors[c.sensor].base_table, c.material);
+        sample_freq<S>(P, p, rs, sensors_of<S>(P)[c.sensor].base_table, c.material);
         float r1 = rs.uf();
         float r2 = rs.uf();
         if (r1 + r2 > 1.f) {
@@ -156,7 +177,7 @@ template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, P
         iso_dir(p, rs);
         return P.dt;
     }
-    const EmitterDev& e = P.emitters[static_cast<std::uint32_t>(-(g.source + 1))];
+    const EmitterDev& e = emitters_of<S>(P)[static_cast<std::uint32_t>(-(g.source + 1))];
     const float t_birth = g.t0 + g.span * rs.uf();
     const bool phasor = P.phasor_sim != 0;
     p.meta = make_meta(e.cell, e.edge, 0, g.sign, phasor);
@@ -208,6 +229,9 @@ template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P,
         L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
         L.rs.init(P.key0, P.key1, P.step, L.p.id);
         L.rem = P.dt;
+        // A phonon that scatters or draws a new scattering time in this step needs random words:
+        // make them here, where most lanes of the warp start a step together.
+        if (L.p.tts < L.rem) { L.rs.prefill(); }
     } else {
         L.rem = spawn32<S>(P, L.p, L.rs, i - n_alive);
     }
@@ -236,7 +260,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
             p.tts = fmaxf(p.tts, 0.f);
         }
         if (p.tts <= 0.f) {// time to the next scattering event (modelSimulator.cpp:148-153)
-            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
+            const float3 r = rates32(materials_of<S>(P)[L.mat], sensors_of<S>(P)[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
             const float sum = r.x + r.y + r.z;
             const float inv = __frcp_rn(r.x + r.y + r.z);
             p.tts = 1e9f * (-__logf(rs.uf())) * inv;
@@ -286,7 +310,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
             const CellF32* N = cells_of<S>(P) + link;
             bool pass = true;
             if (N->material != L.mat) {
-                const MaterialDev& mt = P.materials[N->material];
+                const MaterialDev& mt = materials_of<S>(P)[N->material];
                 const float w = omega32<S>(P, p.binw, phasor);
                 pass = !(w > (meta_pol(p.meta) == 0 ? mt.w_max_la : mt.w_max_ta));
             }
@@ -308,7 +332,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
         } else if (link == -1) {
             reflect(p, rs, C->spec, E);
         } else {// EmitSurface::handlePhonon (psim/src/surface.cpp:61-65)
-            const EmitterDev& em = P.emitters[static_cast<std::uint32_t>(-(link + 2))];
+            const EmitterDev& em = emitters_of<S>(P)[static_cast<std::uint32_t>(-(link + 2))];
             if (P.step >= em.absorb_lo && P.step <= em.absorb_hi) {
                 out = Outcome{ false, false, false, 0U, 0, 0 };
                 return true;// absorbed
@@ -354,14 +378,14 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
     }
     if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
         if (!L.rates_ok) {// the scattering time was drawn in an earlier step: recompute its rates
-            const float3 r = rates32(P.materials[L.mat], P.sensors[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
+            const float3 r = rates32(materials_of<S>(P)[L.mat], sensors_of<S>(P)[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
             const float inv = __frcp_rn(r.x + r.y + r.z);
             L.fN = r.x * inv;
             L.fNU = (r.x + r.y) * inv;
         }
         const float u = rs.uf();
         if (u <= L.fNU) {// normal or Umklapp: resample frequency, velocity and polarization
-            sample_freq<S>(P, p, rs, P.sensors[L.sensor].scatter_table, L.mat);
+            sample_freq<S>(P, p, rs, sensors_of<S>(P)[L.sensor].scatter_table, L.mat);
             L.v = vel32<S>(P, p.binw, meta_pol(p.meta), phasor);
             if (u > L.fN) {// Umklapp: also a new direction
                 iso_dir(p, rs);
@@ -392,7 +416,13 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
             const unsigned alias_b = (P.stage_mask & 2U) ? P.n_tables * kAliasCols * 4U : 0U;
             const unsigned vel_b = (P.stage_mask & 4U) ? P.n_materials * 2U * kBins * 4U : 0U;
             const unsigned centre_b = (P.stage_mask & 4U) ? P.n_materials * kBins * 4U : 0U;
-            mbar_expect_tx(&stage_bar, cells_b + alias_b + vel_b + centre_b);
+            const unsigned sens_b = P.n_sensors * static_cast<unsigned>(sizeof(SensorDev));
+            const unsigned mat_b = P.n_materials * static_cast<unsigned>(sizeof(MaterialDev));
+            const unsigned emit_b = P.n_emitters * static_cast<unsigned>(sizeof(EmitterDev));
+            mbar_expect_tx(&stage_bar, cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b);
+            bulk_to_shared(g_smem + P.off_sensors, P.sensors, sens_b, &stage_bar);
+            bulk_to_shared(g_smem + P.off_materials, P.materials, mat_b, &stage_bar);
+            if (emit_b != 0U) { bulk_to_shared(g_smem + P.off_emitters, P.emitters, emit_b, &stage_bar); }
             if (cells_b != 0U) { bulk_to_shared(g_smem + P.off_cells, P.cells32, cells_b, &stage_bar); }
             if (alias_b != 0U) { bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, &stage_bar); }
             if (vel_b != 0U) {
