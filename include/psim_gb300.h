@@ -222,6 +222,30 @@ int psim_interpret(const psim_interp_desc* d, const int64_t* energy, const doubl
 /* getFinalTemp(sensor, start_step) for every sensor: out[S]. */
 int psim_final_temps(const psim_interp_desc* d, const int64_t* energy, uint64_t start_step, double* out);
 
+/* psim_final_temps without any allocation.  This has no counterpart in the reference.
+ * It is for hosts that must not allocate device memory inside a call: a host that keeps
+ * all device memory in its own pool, or that runs under a hard device-memory quota.
+ *
+ * energy_dev[S][K] (raw tallies) and out_dev[S] are DEVICE pointers owned by the caller; the
+ * work is enqueued on cuda_stream (a cudaStream_t of the current device, NULL = legacy default
+ * stream) and the call returns without waiting for it.  The descriptor's host arrays are copied
+ * to the device with cudaMemcpyAsync: from pageable memory they may be reused once the call
+ * returns, from pinned memory only once the stream has passed the call.  Results equal
+ * psim_final_temps on the same tallies.
+ *
+ * Limit: the tables plus the per-step temperatures (S x (K - start_step) x 8 bytes, each part
+ * rounded up to 256 bytes) must fit in one fixed device scratch of
+ * psim_final_temps_noalloc_max_bytes() bytes (8 MiB); larger inputs fail with PSIM_ERR_LIMIT
+ * before anything is enqueued.  The scratch is one per device and per process: calls whose GPU
+ * work overlaps (different streams, or several host threads) race on it and give wrong results;
+ * order them on one stream or with events.  The first call on each device looks up the
+ * scratch's address (and may load the module onto that device): make it before any stream
+ * capture. */
+int psim_final_temps_noalloc(const psim_interp_desc* d, const int64_t* energy_dev, uint64_t start_step,
+                             double* out_dev, void* cuda_stream);
+/* Size in bytes of the fixed scratch behind psim_final_temps_noalloc. */
+uint64_t psim_final_temps_noalloc_max_bytes(void);
+
 /* ------------------------------------------------------------------------------------------
  * FP64 geometry on the GPU, bit-exact with the reference routines.
  * ------------------------------------------------------------------------------------------ */

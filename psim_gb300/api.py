@@ -109,6 +109,9 @@ SIGNATURES = {
     "psim_sim_destroy": (None, [ctypes.c_void_p]),
     "psim_interpret": (ctypes.c_int, [ctypes.POINTER(InterpDesc), _c_i64p, _c_dp, _c_dp, _c_dp, _c_dp]),
     "psim_final_temps": (ctypes.c_int, [ctypes.POINTER(InterpDesc), _c_i64p, ctypes.c_uint64, _c_dp]),
+    "psim_final_temps_noalloc": (ctypes.c_int, [ctypes.POINTER(InterpDesc), ctypes.c_void_p, ctypes.c_uint64,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "psim_final_temps_noalloc_max_bytes": (ctypes.c_uint64, []),
     "psim_geom_intersect": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
@@ -315,6 +318,18 @@ def final_temps(desc: InterpDesc, energy: np.ndarray, start_step: int) -> np.nda
     out = np.zeros(desc.n_sensors)
     _check(lib().psim_final_temps(ctypes.byref(desc), _i64(energy), start_step, _dp(out)))
     return out
+
+
+def final_temps_noalloc(desc: InterpDesc, energy_dev: int, start_step: int, out_dev: int,
+                        stream: Optional[int] = None) -> None:
+    """psim_final_temps_noalloc: device addresses in (int64 [S][K]) and out (float64 [S]),
+    enqueued on ``stream`` (a cudaStream_t as an int) without waiting for it."""
+    _check(lib().psim_final_temps_noalloc(ctypes.byref(desc), ctypes.c_void_p(energy_dev), start_step,
+                                          ctypes.c_void_p(out_dev), ctypes.c_void_p(stream)))
+
+
+def final_temps_noalloc_max_bytes() -> int:
+    return int(lib().psim_final_temps_noalloc_max_bytes())
 
 
 def geom_intersect(a: np.ndarray, b: np.ndarray):

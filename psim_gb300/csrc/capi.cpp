@@ -371,6 +371,30 @@ int psim_final_temps(const psim_interp_desc* d, const int64_t* energy, uint64_t 
     return guard([&]() { psim::gpu::final_temps_host(interp_from(d), energy, start_step, out); });
 }
 
+int psim_final_temps_noalloc(const psim_interp_desc* d, const int64_t* energy_dev, uint64_t start_step, double* out_dev,
+                             void* cuda_stream) {
+    if (d == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    return guard([&]() {
+        psim::gpu::InterpView v;
+        v.n_sensors = d->n_sensors;
+        v.recorded = d->recorded_steps;
+        v.t_eq = d->t_eq;
+        v.eff_energy = d->eff_energy;
+        v.lb = d->lower_bound;
+        v.ub = d->upper_bound;
+        v.area = d->sensor_area;
+        v.heat_capacity = d->sensor_heat_capacity;
+        v.material = d->sensor_material;
+        v.n_materials = d->n_materials;
+        v.mat_temp_begin = d->mat_temp_begin;
+        v.temps = d->temps;
+        v.energies = d->energies;
+        psim::gpu::final_temps_noalloc(v, energy_dev, start_step, out_dev, cuda_stream);
+    });
+}
+
+uint64_t psim_final_temps_noalloc_max_bytes(void) { return psim::gpu::kFinalTempsScratchBytes; }
+
 // ------------------------------------------------------------------ geometry
 int psim_geom_intersect(int64_t n, const double* a, const double* b, double* poi, int32_t* has) {
     if (n < 0 || (n > 0 && (a == nullptr || b == nullptr || poi == nullptr || has == nullptr))) { return fail(PSIM_ERR_INVALID, "bad arguments"); }

@@ -122,6 +122,30 @@ void interpret_host(const InterpDesc& d, const std::int64_t* energy, const doubl
                     double* stats);
 void final_temps_host(const InterpDesc& d, const std::int64_t* energy, std::uint64_t start, double* out);
 
+// Interpreter inputs as the caller's own host arrays, for the call that allocates nothing.
+struct InterpView {
+    std::uint32_t n_sensors{ 0 };
+    std::uint64_t recorded{ 0 };
+    double t_eq{ 0. }, eff_energy{ 0. }, lb{ 0. }, ub{ 0. };
+    const double* area{ nullptr };
+    const double* heat_capacity{ nullptr };
+    const std::uint32_t* material{ nullptr };
+    std::uint32_t n_materials{ 0 };
+    const std::uint64_t* mat_temp_begin{ nullptr };// [n_materials + 1]
+    const double* temps{ nullptr };
+    const double* energies{ nullptr };
+};
+
+// Size of the fixed device scratch behind final_temps_noalloc.
+constexpr std::size_t kFinalTempsScratchBytes = std::size_t{ 8 } << 20;
+// Scratch bytes final_temps_noalloc needs for these inputs (tables plus S x (K - start) doubles).
+std::size_t final_temps_scratch_bytes(const InterpView& d, std::uint64_t start);
+// getFinalTemp for every sensor with device-resident tallies energy_dev[S][K] and result
+// out_dev[S], enqueued on `stream` (a cudaStream_t; NULL = legacy default stream).  Uses the
+// module's static scratch instead of allocating; throws std::length_error past its size.
+void final_temps_noalloc(const InterpView& d, const std::int64_t* energy_dev, std::uint64_t start, double* out_dev,
+                         void* stream);
+
 // FP64 geometry kernels (bit-exact with the reference routines).
 void geom_intersect(std::int64_t n, const double* a, const double* b, double* poi, std::int32_t* has);
 void geom_on_line(std::int64_t n, const double* lines, const double* pts, std::int32_t* out);

@@ -4,6 +4,9 @@
 // reference's host arithmetic on the same tallies.
 #include <cuda_runtime.h>
 
+#include <climits>
+#include <cstdint>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -238,6 +241,119 @@ void final_temps_host(const InterpDesc& d, const std::int64_t* energy, std::uint
     DevBuf e(SK * sizeof(long long));
     check(cudaMemcpy(e.p, energy, SK * sizeof(long long), cudaMemcpyHostToDevice), "upload energy");
     final_temps_device(d, e.as<long long>(), start, out, nullptr);
+}
+
+// ---------------------------------------------------------------- final temperatures without allocation
+// The same two kernels as final_temps_device, with every intermediate buffer carved out of
+// one fixed, module-scope device array instead of cudaMalloc.  It serves callers that must
+// not allocate device memory during a call: a host that keeps all device memory in its own
+// pool, or that runs under a hard device-memory quota.
+namespace {
+
+// Holds, each aligned to 256 bytes: sensor areas, heat capacities and materials, the material
+// offsets, the temperature grid and tabulated energies, then S x (K - start) temperatures.
+// Nothing in it has to start at zero: every byte a call reads, the same call writes first.
+static __device__ __align__(256) unsigned char g_final_temps_scratch[kFinalTempsScratchBytes];
+
+constexpr int kMaxScratchDevices = 64;
+std::mutex g_scratch_mu;
+unsigned char* g_scratch_ptr[kMaxScratchDevices] = {};
+
+// Device address of the scratch on the current device, looked up on the first call per device
+// (which may load this module onto that device).
+unsigned char* scratch_for_current_device() {
+    int dev = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxScratchDevices) { throw std::invalid_argument("device ordinal beyond the scratch table"); }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (g_scratch_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        check(cudaGetSymbolAddress(&p, g_final_temps_scratch), "cudaGetSymbolAddress(final temps scratch)");
+        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_scratch_ptr[dev];
+}
+
+constexpr std::size_t round256(std::size_t n) { return (n + 255) & ~std::size_t{ 255 }; }
+
+// Validates the view and returns its table sizes; throws std::invalid_argument.
+std::uint64_t checked_grid_size(const InterpView& d, std::uint64_t start) {
+    if (start > d.recorded) { throw std::invalid_argument("start step beyond the recorded steps"); }
+    if (d.n_sensors == 0) { return 0; }
+    if (d.area == nullptr || d.heat_capacity == nullptr || d.material == nullptr || d.mat_temp_begin == nullptr) {
+        throw std::invalid_argument("missing sensor or material array");
+    }
+    if (d.n_materials == 0) { throw std::invalid_argument("no materials"); }
+    for (std::uint32_t m = 0; m < d.n_materials; ++m) {
+        if (d.mat_temp_begin[m + 1] < d.mat_temp_begin[m]) { throw std::invalid_argument("mat_temp_begin decreases"); }
+    }
+    for (std::uint32_t s = 0; s < d.n_sensors; ++s) {
+        const std::uint32_t m = d.material[s];
+        if (m >= d.n_materials) { throw std::invalid_argument("sensor material out of range"); }
+        if (d.mat_temp_begin[m + 1] <= d.mat_temp_begin[m]) { throw std::invalid_argument("material has an empty temperature grid"); }
+    }
+    const std::uint64_t nt = d.mat_temp_begin[d.n_materials];
+    if (nt > 0 && (d.temps == nullptr || d.energies == nullptr)) { throw std::invalid_argument("missing temperature grid"); }
+    return nt;
+}
+
+}// namespace
+
+std::size_t final_temps_scratch_bytes(const InterpView& d, std::uint64_t start) {
+    const std::uint64_t nt = checked_grid_size(d, start);
+    const std::uint64_t S = d.n_sensors;
+    const std::uint64_t steps = d.recorded - start;
+    const std::uint64_t cap = kFinalTempsScratchBytes;
+    // every term is bounded before it is multiplied, so nothing wraps
+    if (nt > cap || (S > 0 && steps > cap / (S * sizeof(double)))) { return SIZE_MAX; }
+    return 2 * round256(S * sizeof(double)) + round256(S * sizeof(std::uint32_t))
+           + round256((static_cast<std::size_t>(d.n_materials) + 1) * sizeof(std::uint64_t)) + 2 * round256(nt * sizeof(double))
+           + round256(S * steps * sizeof(double));
+}
+
+void final_temps_noalloc(const InterpView& d, const std::int64_t* energy_dev, std::uint64_t start, double* out_dev,
+                         void* stream_handle) {
+    const std::size_t need = final_temps_scratch_bytes(d, start);
+    if (need > kFinalTempsScratchBytes) {
+        throw std::length_error("final temperatures need more than the fixed " + std::to_string(kFinalTempsScratchBytes >> 20)
+                                + " MiB device scratch (tables plus sensors x steps x 8 bytes)");
+    }
+    if (d.n_sensors == 0) { return; }
+    if (out_dev == nullptr || (d.recorded > start && energy_dev == nullptr)) { throw std::invalid_argument("null device buffer"); }
+    auto stream = static_cast<cudaStream_t>(stream_handle);
+    unsigned char* base = scratch_for_current_device();
+    const std::uint64_t S = d.n_sensors;
+    const std::uint64_t nt = d.mat_temp_begin[d.n_materials];
+    std::size_t off = 0;
+    auto place = [&](const void* src, std::size_t bytes) {
+        unsigned char* dst = base + off;
+        off += round256(bytes);
+        if (bytes > 0) { check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream), "copy interpreter tables"); }
+        return dst;
+    };
+    InterpDev dev{};
+    dev.S = d.n_sensors;
+    dev.K = d.recorded;
+    dev.t_eq = d.t_eq;
+    dev.eff = d.eff_energy;
+    dev.lb = d.lb;
+    dev.ub = d.ub;
+    dev.area = reinterpret_cast<const double*>(place(d.area, S * sizeof(double)));
+    dev.heat = reinterpret_cast<const double*>(place(d.heat_capacity, S * sizeof(double)));
+    dev.init_temp = nullptr;
+    dev.material = reinterpret_cast<const std::uint32_t*>(place(d.material, S * sizeof(std::uint32_t)));
+    dev.mtb = reinterpret_cast<const std::uint64_t*>(
+        place(d.mat_temp_begin, (static_cast<std::size_t>(d.n_materials) + 1) * sizeof(std::uint64_t)));
+    dev.temps = reinterpret_cast<const double*>(place(d.temps, nt * sizeof(double)));
+    dev.energies = reinterpret_cast<const double*>(place(d.energies, nt * sizeof(double)));
+    double* tvals = reinterpret_cast<double*>(base + off);
+    const std::uint64_t n = S * (d.recorded - start);
+    if (n > 0) {
+        temps_kernel<<<std::max(1, blocks_for(n, 256)), 256, 0, stream>>>(dev, reinterpret_cast<const long long*>(energy_dev),
+                                                                           start, tvals);
+    }
+    final_kernel<<<std::max(1U, (d.n_sensors + 127) / 128), 128, 0, stream>>>(dev, tvals, start, out_dev);
+    check(cudaGetLastError(), "final temps kernels");
 }
 
 // ---------------------------------------------------------------- FP64 geometry check kernels
