@@ -60,26 +60,18 @@ def barrier(dist):
 
 
 def reduce_max(dist, value: float) -> float:
-    if dist is None:
-        return value
-    import torch
-    t = torch.tensor([value], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from psim_gb300 import shard
+    return shard.reduce_max(value, dist)
 
 
 def reduce_sum(dist, value: float) -> float:
-    if dist is None:
-        return value
-    import torch
-    t = torch.tensor([value], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    from psim_gb300 import shard
+    return shard.reduce_sum(value, dist)
 
 
-def model_json(path: str, num_phonons: int, steps: int = STEPS) -> str:
+def model_json(path: str, num_phonons: int, steps: int = STEPS, dt_ps: float = DT_PS) -> str:
     from psim_gb300 import modelgen as mg
-    m = mg.kinked(seed=0, num_phonons=int(num_phonons), num_measurements=steps, sim_time=steps * DT_PS * 1e-3,
+    m = mg.kinked(seed=0, num_phonons=int(num_phonons), num_measurements=steps, sim_time=steps * dt_ps * 1e-3,
                   step_interval=50)
     return mg.write(m, path)
 
@@ -163,7 +155,6 @@ def run_reference(args, rank, world):
             steps += n
             secs += s
     rate = steps / secs
-    src = "oracle/_ref (the reference built from source)" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "ref_driver")) else "oracle port"
     line = {
         "impl": "reference", "metric": "phonon-steps/s", "value": rate, "unit": "phonon-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
@@ -171,8 +162,9 @@ def run_reference(args, rank, world):
         "config": {"workload": "kinked 3-arm, 400 cells/sensors, periodic, dt 2 ps, 5000 steps",
                    "num_phonons": budget, "sample": f"budget {budget} phonons (bounded CPU sample)"},
         "cpu_baseline": {"value": rate, "unit": "phonon-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"kinked model, 5000 steps, {budget}-phonon budget per run; {src} is not available "
-                                   f"on this host, the bit-exact C++ restatement (oracle/) runs instead"},
+                         "sample": f"kinked model, 5000 steps, {budget}-phonon budget per run, on {threads} host threads; "
+                                   "the reference built from its sources (oracle/_ref) cannot be built without them, so "
+                                   "the bit-exact C++ restatement of its algorithm (oracle/) runs"},
         "e2e": {"value": rate, "unit": "phonon-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -187,6 +179,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--per-step", type=float, default=PER_STEP)
     ap.add_argument("--measurements", type=int, default=STEPS)
+    ap.add_argument("--dt-ps", type=float, default=DT_PS, help="measurement step length in ps")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cpu-budget", type=int, default=3000000)
     ap.add_argument("--population-out", default="", help="write the phonon population per step of the last timed run (JSON)")
@@ -200,24 +193,26 @@ def main():
     import torch
     torch.cuda.set_device(local)
     dist = init_dist(world, "nccl")
-    from psim_gb300 import api, build
+    from psim_gb300 import api, build, shard
+    # the once-per-run tally exchange runs on host buffers: a gloo group beside NCCL
+    tally_group = dist.new_group(backend="gloo") if dist is not None else None
     build.build()
     precision = api.FP64 if args.precision == "fp64" else api.FP32
     steps_n = args.measurements
     td = tempfile.mkdtemp(prefix="psim_bench_")
 
     # pilot run (untimed): mean lifetime in steps -> phonon budget for the target population
-    pilot = api.Model(model_json(os.path.join(td, "pilot.json"), 200000, steps_n))
-    pilot.run(seed=99 + rank, precision=precision)
+    pilot = api.Model(model_json(os.path.join(td, "pilot.json"), 200000, steps_n, args.dt_ps))
+    pilot.run(seed=shard.rank_seed(99, rank), precision=precision)
     pc = pilot.counters()
     lifetime = pc["phonon_steps"] / max(pc["phonons"], 1)
     budget = int(args.per_step * steps_n / lifetime)
-    path = model_json(os.path.join(td, "kinked.json"), budget, steps_n)
+    path = model_json(os.path.join(td, "kinked.json"), budget, steps_n, args.dt_ps)
     model = api.Model(path)
 
     stream = torch.cuda.Stream()
     for w in range(args.warmup):
-        model.run(seed=1000 * (rank + 1) + w, precision=precision, stream=stream.cuda_stream)
+        model.run(seed=shard.rank_seed(1000 + w, rank), precision=precision, stream=stream.cuda_stream)
 
     # ---- timed: device-resident runs
     clocks = ClockSampler(os.path.join(td, "clocks.csv"))
@@ -232,7 +227,9 @@ def main():
     t0 = time.perf_counter()
     ev0.record(stream)
     for k in range(args.steps):
-        model.run(seed=7000 * (rank + 1) + k, precision=precision, stream=stream.cuda_stream)
+        model.run(seed=shard.rank_seed(7000 + k, rank), precision=precision, stream=stream.cuda_stream)
+        if dist is not None:
+            shard.combine_tallies(*model.tallies(), dist, tally_group)
         c = model.counters()
         phonon_steps += c["phonon_steps"]
         kernel_ms += c["kernel_ms"]
@@ -275,7 +272,9 @@ def main():
         t0 = time.perf_counter()
         for k in range(args.steps):
             m = api.Model(path)
-            m.run(seed=9000 * (rank + 1) + k, precision=precision)
+            m.run(seed=shard.rank_seed(9000 + k, rank), precision=precision)
+            if dist is not None:
+                shard.combine_tallies(*m.tallies(), dist, tally_group)
             stats = m.measurements()
             temps, fluxes = m.series(0)
             c = m.counters()
@@ -304,7 +303,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == api.FP32 else "f64",
             "data": "synthetic",
-            "config": {"workload": "kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt 2 ps, "
+            "config": {"workload": f"kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt {args.dt_ps:g} ps, "
                                    f"{steps_n} steps, output every 50 steps, {args.per_step:.0e} phonons per step",
                        "num_phonons_per_rank": budget, "mean_lifetime_steps": lifetime,
                        "mean_population": phonon_steps / args.steps / steps_n,

@@ -73,23 +73,13 @@ def test_counters_and_phonon_steps(api):
 def test_seam_matches_model_statistically(api):
     """psim_sim_* driven directly (the ModelSimulator seam) with the model's own description
     and emitter energies taken from the reference's tables gives the reference's result."""
-    gold_t = np.load(os.path.join(GOLDEN, "tables_bar_ss.npz"))
     gold_r = np.load(os.path.join(GOLDEN, "runs_bar_ss.npz"))["stats"]
     m = api.Model(model_path("bar_ss"))
     d = m.sim_desc()
     sim = api.Simulator(d)
     idesc = m.interp_desc()
-    E = d.n_emitters
-    temps = gold_t["temps"]
-    lines = np.ctypeslib.as_array(d.emit_line, shape=(E, 4))
-    et = np.ctypeslib.as_array(d.emit_temp, shape=(E,))
-    dur = np.ctypeslib.as_array(d.emit_duration, shape=(E,))
     t_eq = idesc.t_eq
-    emit = np.zeros(E)
-    for e in range(E):
-        k = int(np.searchsorted(temps, et[e]))
-        length = np.hypot(lines[e, 2] - lines[e, 0], lines[e, 3] - lines[e, 1])
-        emit[e] = gold_t["emit_sum"][k] * dur[e] * length / 4.0 * abs(t_eq - et[e])
+    emit = emit_energies_bar_ss(d, t_eq)
     cell = np.zeros(d.n_cells)  # the sensors start at t_eq: no initial phonons
     S = d.n_sensors
     init_t = np.ctypeslib.as_array(idesc.sensor_init_temp, shape=(S,)).copy()
@@ -110,6 +100,59 @@ def test_seam_matches_model_statistically(api):
     t_ref = gold_r[:, :, 0].mean(axis=0)
     assert np.all(np.diff(t_got) < 0) and np.all(np.diff(t_ref) < 0)
     assert np.corrcoef(t_got, t_ref)[0, 1] > 0.99
+
+
+def test_two_shards_match_one_job(api):
+    """A job split over two ranks (run one after the other on this device, tallies summed as
+    the all-reduce would) has the unsplit job's expected temperatures and phonon count."""
+    from psim_gb300 import shard
+    m = api.Model(model_path("bar_ss"))
+    d = m.sim_desc()
+    idesc = m.interp_desc()
+    sim = api.Simulator(d)
+    t_eq, eff = idesc.t_eq, idesc.eff_energy
+    emit = emit_energies_bar_ss(d, t_eq)
+    cell = np.zeros(d.n_cells)
+    init_t = np.ctypeslib.as_array(idesc.sensor_init_temp, shape=(d.n_sensors,)).copy()
+    one, two, n_one, n_two = [], [], [], []
+    for seed in range(1, 9):
+        sim.reset()
+        n_one.append(sim.init_phonon_builders(t_eq, eff, cell, emit, init_t, seed))
+        sim.run(t_eq)
+        e, f = sim.tallies()
+        one.append(api.interpret(idesc, e, f)[2][:, 0])
+        counts = []
+
+        def rank(r):
+            sim.reset()
+            counts.append(sim.init_phonon_builders(t_eq, shard.rank_eff_energy(eff, 2), cell, emit, init_t,
+                                                   shard.rank_seed(100 + seed, r)))
+            sim.run(t_eq)
+            return sim.tallies()
+
+        e, f = shard.local_world(2, rank)
+        n_two.append(sum(counts))
+        two.append(api.interpret(idesc, e, f)[2][:, 0])
+    one, two = np.array(one), np.array(two)
+    assert abs(np.mean(n_two) / np.mean(n_one) - 1) < 0.01
+    se = np.sqrt(one.var(axis=0, ddof=1) / len(one) + two.var(axis=0, ddof=1) / len(two))
+    z = (one.mean(axis=0) - two.mean(axis=0)) / np.maximum(se, 1e-9)
+    assert np.abs(z).max() < 4.5, z
+
+
+def emit_energies_bar_ss(d, t_eq):
+    """Emitter energies from the reference's tables (as the ModelSimulator seam receives them)."""
+    gold_t = np.load(os.path.join(GOLDEN, "tables_bar_ss.npz"))
+    E = d.n_emitters
+    lines = np.ctypeslib.as_array(d.emit_line, shape=(E, 4))
+    et = np.ctypeslib.as_array(d.emit_temp, shape=(E,))
+    dur = np.ctypeslib.as_array(d.emit_duration, shape=(E,))
+    emit = np.zeros(E)
+    for e in range(E):
+        k = int(np.searchsorted(gold_t["temps"], et[e]))
+        length = np.hypot(lines[e, 2] - lines[e, 0], lines[e, 3] - lines[e, 1])
+        emit[e] = gold_t["emit_sum"][k] * dur[e] * length / 4.0 * abs(t_eq - et[e])
+    return emit
 
 
 def test_export_writes_reference_format(api):
