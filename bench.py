@@ -224,6 +224,7 @@ def main():
     phonon_steps = 0
     kernel_ms = 0.0
     launches = 0
+    transport_launches = 0
     t0 = time.perf_counter()
     ev0.record(stream)
     for k in range(args.steps):
@@ -234,6 +235,7 @@ def main():
         phonon_steps += c["phonon_steps"]
         kernel_ms += c["kernel_ms"]
         launches += c["kernel_launches"]
+        transport_launches += c["transport_launches"]
     ev1.record(stream)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -249,9 +251,11 @@ def main():
     value = total_steps / kernel_s
     ms_per_step = 1e3 * reduce_max(dist, span_ms / 1e3) / args.steps
 
-    # roofline of the dominant kernel (the FP32/FP64 transport step)
-    per_launch_bytes = phonon_steps / launches * BYTES_PER_PHONON_STEP * (2 if precision == api.FP64 else 1)
-    avg_launch_s = kernel_ms / 1e3 / launches
+    # roofline of the dominant kernel (the FP32/FP64 transport step): 64 B per phonon-step (one
+    # 32-byte state record read and one written) times the phonon-steps one launch covers; an FP32
+    # launch covers several measurement steps, keeping phonons in registers across the inner ones
+    per_launch_bytes = phonon_steps / transport_launches * BYTES_PER_PHONON_STEP * (2 if precision == api.FP64 else 1)
+    avg_launch_s = kernel_ms / 1e3 / transport_launches
     peak, peak_kind = peaks()
     achieved = per_launch_bytes / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -260,7 +264,7 @@ def main():
     profile = os.path.join(ROOT, "profiles", f"traffic_step_kernel_{args.precision}_kinked.json")
     if os.path.exists(profile):
         tr = json.load(open(profile))
-        roofline["traffic"] = tr.get("dram_bytes_per_phonon_step", 0) * phonon_steps / launches
+        roofline["traffic"] = tr.get("dram_bytes_per_phonon_step", 0) * phonon_steps / transport_launches
         roofline["traffic_source"] = tr.get("source")
 
     # ---- e2e through the public C ABI with host buffers
@@ -308,7 +312,8 @@ def main():
                        "num_phonons_per_rank": budget, "mean_lifetime_steps": lifetime,
                        "mean_population": phonon_steps / args.steps / steps_n,
                        "l2": "inputs larger than L2 (phonon state 2 x 32 B x population)",
-                       "precision": args.precision, "bench_step": "one full simulation run"},
+                       "precision": args.precision, "bench_step": "one full simulation run",
+                       "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
             "clocks": clk, "wall_s_timed": wall,
         }

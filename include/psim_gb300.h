@@ -65,6 +65,8 @@ typedef struct psim_run_counters {
     uint64_t event_limit_hits; /* phonon-steps cut short by the per-step event bound (numerical corner cases) */
     uint64_t h2d_bytes;      /* host-to-device bytes copied by the last run */
     uint64_t d2h_bytes;      /* device-to-host bytes copied by the last run and its read-outs */
+    uint64_t transport_launches; /* launches of the phonon transport kernel (an FP32 launch covers several steps) */
+    uint64_t steps_per_launch;   /* measurement steps per transport launch in the last run (FP64: 1) */
 } psim_run_counters;
 
 /* InputManager::deserialize (psim/src/inputManager.cpp:14-115): reads and validates the model

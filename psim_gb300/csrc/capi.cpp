@@ -143,6 +143,8 @@ int psim_model_counters(const psim_model* m, psim_run_counters* out) {
     out->event_limit_hits = c.event_limits;
     out->h2d_bytes = c.h2d_bytes;
     out->d2h_bytes = c.d2h_bytes;
+    out->transport_launches = c.transport_launches;
+    out->steps_per_launch = c.steps_per_launch;
     return PSIM_OK;
 }
 
@@ -324,6 +326,8 @@ int psim_sim_counters(const psim_sim* s, psim_run_counters* out) {
     out->event_limit_hits = c.event_limits;
     out->h2d_bytes = c.h2d_bytes;
     out->d2h_bytes = c.d2h_bytes;
+    out->transport_launches = c.transport_launches;
+    out->steps_per_launch = c.steps_per_launch;
     return PSIM_OK;
 }
 

@@ -83,6 +83,13 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, std::uint32_t k0, std::uint32_
     return c;
 }
 
+// One Philox block for (block, step, id) of a stream.  Not inlined: the transport kernels draw at
+// a dozen places, and one shared copy of the rounds keeps their code small.
+static __device__ __noinline__ U4 philox_block(std::uint32_t block, std::uint32_t step, std::uint32_t id, std::uint32_t k0,
+                                               std::uint32_t k1) {
+    return philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
+}
+
 // Per-phonon stream for one step: four 32-bit words per Philox call, refilled on demand.  The
 // words shift through registers (no indexed array, so nothing spills to local memory).
 struct Stream {
@@ -102,7 +109,7 @@ struct Stream {
     }
     // Compute the next block of four words now (used where many lanes start a step together).
     __device__ __forceinline__ void prefill() {
-        const U4 r = philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
+        const U4 r = philox_block(block, step, id, k0, k1);
         b0 = r.x;
         b1 = r.y;
         b2 = r.z;
@@ -112,7 +119,7 @@ struct Stream {
     }
     __device__ __forceinline__ std::uint32_t next() {
         if (left == 0) {
-            const U4 r = philox4x32_10(U4{ block, step, id, 0x7073696DU }, k0, k1);
+            const U4 r = philox_block(block, step, id, k0, k1);
             b0 = r.x;
             b1 = r.y;
             b2 = r.z;
@@ -224,6 +231,9 @@ struct alignas(8) TallySlot {
     long long fy;
 };
 
+// Measurement steps one FP32 launch may cover (the shared-memory tally holds one slot per step).
+constexpr std::uint32_t kMaxFused = 8;
+
 struct StepParams {
     // model
     const CellF32* cells32;
@@ -243,6 +253,13 @@ struct StepParams {
     std::uint32_t group_begin, group_end;
     std::uint32_t n_new;
     std::uint32_t id_base;
+    // FP32 launches cover steps [step, step + n_fused).  Work items are the survivors entering
+    // 'step', then the newborns of each covered step j at [new_begin[j], new_begin[j+1]) after
+    // them, with ids from id_base_f[j] and birth groups [group_begin_f[j], group_begin_f[j+1]).
+    std::uint32_t n_fused;
+    std::uint32_t new_begin[kMaxFused + 1];
+    std::uint32_t id_base_f[kMaxFused];
+    std::uint32_t group_begin_f[kMaxFused + 1];
     // state buffers
     const void* in;
     void* out;
@@ -252,7 +269,7 @@ struct StepParams {
     std::uint32_t* count_clear;
     std::uint32_t* work;              // this step's work counter (phonons handed to lanes)
     std::uint32_t* work_clear;        // the counter of two steps ahead, cleared by this step
-    std::uint32_t* population;        // [n_steps] phonons in flight per step (may be null)
+    std::uint32_t* population;        // [n_steps] phonons in flight per step (FP32: accumulated, zeroed per run)
     // Shared-memory staging of read-only tables (FP32 kernel): bit 0 cells, 1 alias tables,
     // 2 velocities + bin centres; byte offsets of each staged segment and of the tallies.
     std::uint32_t stage_mask;
@@ -260,7 +277,7 @@ struct StepParams {
     std::uint32_t off_sensors, off_materials, off_emitters, n_emitters;
     std::uint32_t n_cells, n_tables, n_materials;
     // step
-    std::uint32_t step;               // 0-based step index; phonons alive at its end reach boundary step+1
+    std::uint32_t step;               // 0-based (first) step; phonons alive at its end reach boundary step+1
     std::uint32_t n_steps;
     std::uint32_t step_adj;           // first tallied boundary
     std::uint32_t n_recorded;

@@ -21,6 +21,7 @@
 namespace psim::gpu {
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
+void launch_population_max(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters, cudaStream_t stream);
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
 int occupancy_f32(bool staged, int block, std::size_t smem);
 int occupancy_f64(std::size_t smem);
@@ -518,6 +519,7 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
     check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
+    check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
 
     StepParams P{};
     P.cells32 = I.cells32.as<CellF32>();
@@ -549,8 +551,14 @@ void Engine::run(int precision, void* stream_ptr) {
     auto* counts = I.counts.as<std::uint32_t>();
     // Launch shape and shared memory.  The FP32 kernel stages the cell records and the
     // alias / velocity / bin-centre tables into shared memory (TMA bulk copies) when they fit
-    // next to the block's tally, and then runs one 1024-thread block per SM.
-    const std::size_t tally_b = tally_smem_bytes(d.n_sensors);
+    // next to the block's tally, and then runs one 1024-thread block per SM.  An FP32 launch
+    // covers as many steps (up to kMaxFused) as tally slots fit in the shared memory left.
+    std::uint32_t fuse_cap = kMaxFused;
+    if (const char* f = std::getenv("PSIM_GB300_FUSE"); f != nullptr && std::atoi(f) > 0) {
+        fuse_cap = std::min<std::uint32_t>(kMaxFused, static_cast<std::uint32_t>(std::atoi(f)));
+    }
+    std::uint32_t fused = 1;
+    std::size_t tally_b = tally_smem_bytes(d.n_sensors, 1);
     P.n_cells = d.n_cells;
     P.n_tables = d.n_tables;
     P.n_materials = d.n_materials;
@@ -576,6 +584,8 @@ void Engine::run(int precision, void* stream_ptr) {
         const std::size_t emit_b = static_cast<std::size_t>(d.n_emitters) * sizeof(EmitterDev);
         const std::size_t used = cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b;
         if (used + tally_b <= budget) {// everything or nothing: the staged kernel reads every table from shared memory
+            while (fused < fuse_cap && used + tally_smem_bytes(d.n_sensors, fused + 1) <= budget) { ++fused; }
+            tally_b = tally_smem_bytes(d.n_sensors, fused);
             P.off_cells = 0U;
             P.off_alias = static_cast<std::uint32_t>(cells_b);
             P.off_vel = static_cast<std::uint32_t>(cells_b + alias_b);
@@ -589,38 +599,74 @@ void Engine::run(int precision, void* stream_ptr) {
             block = 1024;
         }
     }
+    // global tables: tally slots up to 32 KB per 256-thread block
+    auto unstaged_fuse = [&]() {
+        fused = 1;
+        while (fused < fuse_cap && tally_smem_bytes(d.n_sensors, fused + 1) <= 32 * 1024) { ++fused; }
+        tally_b = tally_smem_bytes(d.n_sensors, fused);
+        smem = tally_b;
+    };
+    if (!fp64 && P.stage_mask == 0U) { unstaged_fuse(); }
     int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(P.stage_mask != 0U, block, smem);
     if (occ <= 0 && !fp64 && P.stage_mask != 0U) {// cannot launch staged: fall back to global tables
         P.stage_mask = 0U;
         P.off_tally = 0U;
-        smem = tally_b;
         block = 256;
+        unstaged_fuse();
         occ = occupancy_f32(false, block, smem);
     }
+    if (fp64) { fused = 1; }
     occ = std::max(1, occ);
     int grid = grid_override_ > 0 ? grid_override_ : I.sms * occ;
     last_stage_mask_ = P.stage_mask;
     if (const char* g = std::getenv("PSIM_GB300_GRID"); g != nullptr && std::atoi(g) > 0) { grid = std::atoi(g); }// launch-shape override
 
+    // FP32: launch w covers steps [s0, s0 + tw); FP64: one step per launch.
+    std::uint64_t launches = 0;
     auto enqueue = [&]() {
-        for (std::uint64_t s = 0; s < d.steps; ++s) {
-            P.step = static_cast<std::uint32_t>(s);
-            P.in = I.state[s % 2].p;
-            P.out = I.state[(s + 1) % 2].p;
-            P.count_in = counts + (s % 3);
-            P.count_out = counts + ((s + 1) % 3);
-            P.count_clear = counts + ((s + 2) % 3);
-            P.work = counts + 4 + (s % 3);
-            P.work_clear = counts + 4 + ((s + 2) % 3);
-            P.group_begin = I.group_begin[s];
-            P.group_end = I.group_begin[s + 1];
-            P.n_new = I.n_new[s];
-            P.id_base = I.id_base[s];
+        launches = 0;
+        std::uint64_t w = 0;
+        for (std::uint64_t s0 = 0; s0 < d.steps; ++w) {
+            std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, d.steps - s0));
+            // every work item of a launch is numbered in 32 bits
+            auto items = [&](std::uint32_t n) {
+                std::uint64_t t = P.capacity;
+                for (std::uint32_t j = 0; j < n; ++j) { t += I.n_new[s0 + j]; }
+                return t;
+            };
+            while (tw > 1 && items(tw) > 0xFFFFFFFFULL) { --tw; }
+            if (items(tw) > 0xFFFFFFFFULL) { throw std::length_error("too many phonons in one step for 32-bit work indices"); }
+            P.step = static_cast<std::uint32_t>(s0);
+            P.n_fused = tw;
+            P.in = I.state[w % 2].p;
+            P.out = I.state[(w + 1) % 2].p;
+            P.count_in = counts + (w % 3);
+            P.count_out = counts + ((w + 1) % 3);
+            P.count_clear = counts + ((w + 2) % 3);
+            P.work = counts + 4 + (w % 3);
+            P.work_clear = counts + 4 + ((w + 2) % 3);
+            P.group_begin = I.group_begin[s0];
+            P.group_end = I.group_begin[s0 + 1];
+            P.n_new = I.n_new[s0];
+            P.id_base = I.id_base[s0];
+            P.new_begin[0] = 0U;
+            for (std::uint32_t j = 0; j < tw; ++j) {
+                P.new_begin[j + 1] = P.new_begin[j] + I.n_new[s0 + j];
+                P.id_base_f[j] = I.id_base[s0 + j];
+                P.group_begin_f[j] = I.group_begin[s0 + j];
+            }
+            P.group_begin_f[tw] = I.group_begin[s0 + tw];
             if (fp64) {
                 launch_step_f64(P, grid, smem, stream);
             } else {
                 launch_step_f32(P, grid, block, smem, stream);
             }
+            ++launches;
+            s0 += tw;
+        }
+        if (!fp64) {
+            launch_population_max(P.population, static_cast<std::uint32_t>(d.steps), P.counters, stream);
+            ++launches;
         }
     };
 
@@ -655,7 +701,10 @@ void Engine::run(int precision, void* stream_ptr) {
     counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
     counters_.kernel_ms += ms;
     counters_.d2h_bytes += sizeof c;
-    counters_.kernel_launches += d.steps;
+    counters_.kernel_launches += launches;
+    counters_.transport_launches += fp64 ? launches : launches - 1;// FP32 adds one population pass
+    counters_.steps_per_launch = fused;
+    last_fused_ = fused;
     I.builders_ready = false;
     if (c[2] != 0) { throw std::length_error("phonon buffer overflow: the device ran out of memory for the population"); }
 }

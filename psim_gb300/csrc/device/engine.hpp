@@ -53,6 +53,8 @@ struct RunCounters {
     std::uint64_t event_limits{ 0 };
     std::uint64_t h2d_bytes{ 0 };
     std::uint64_t d2h_bytes{ 0 };
+    std::uint64_t transport_launches{ 0 };
+    std::uint64_t steps_per_launch{ 0 };
     double kernel_ms{ 0. };
 };
 
@@ -88,6 +90,8 @@ public:
     // Stage cells and tables into shared memory in the FP32 kernel when they fit (default on).
     void set_stage_tables(bool on) { stage_tables_ = on; }
     std::uint32_t last_stage_mask() const noexcept { return last_stage_mask_; }
+    // Measurement steps per FP32 launch in the last run (1 for FP64).
+    std::uint32_t last_fused() const noexcept { return last_fused_; }
 
     // Phonons in flight at each measurement step of the last run (alive + born), [steps].
     void population(std::uint32_t* out) const;
@@ -114,6 +118,7 @@ private:
     bool use_graph_{ true };
     bool stage_tables_{ true };
     std::uint32_t last_stage_mask_{ 0 };
+    std::uint32_t last_fused_{ 1 };
     int grid_override_{ 0 };
 };
 

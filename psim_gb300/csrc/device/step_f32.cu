@@ -1,10 +1,12 @@
-// FP32 cell-local phonon transport: one launch advances every phonon across one
-// measurement step (ModelSimulator::simulatePhonon, psim/src/modelSimulator.cpp:139-198,
+// FP32 cell-local phonon transport: one launch advances every phonon across up to kMaxFused
+// measurement steps (ModelSimulator::simulatePhonon, psim/src/modelSimulator.cpp:139-198,
 // reorganised step by step instead of phonon by phonon).
 //
-// Per phonon and step: load 32 B of state (or create the phonon if it is born in this
-// step), run events until the step boundary or absorption, tally at the boundary, and
-// write the 32 B survivor record to the compacted output buffer.
+// Per phonon: load 32 B of state (or create the phonon in the step it is born in), run events
+// until a step boundary or absorption, and tally at the boundary.  A phonon that crosses a
+// boundary inside the launch's steps goes on in registers, with the next step's random
+// stream; one that crosses the launch's last boundary is written, 32 B, to the compacted
+// output buffer.  Results do not depend on how many steps a launch covers.
 //
 // Geometry: positions are relative to the cell's first vertex.  The exit time through
 // edge e is (h_e - n_e.p) / (n_e.w) for edges the phonon moves towards (n_e.w > 0), the
@@ -154,12 +156,13 @@ template<bool S> __device__ __forceinline__ void sample_freq(const StepParams& P
     p.meta = meta_with_pol(p.meta, static_cast<int>(o & 1U));
 }
 
-// Create newborn j of this step (CellOriginBuilder / SurfaceOriginBuilder / PhasorBuilder,
-// psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
-template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t j) {
-    const BirthGroup g = P.groups[find_group(P, j)];
-    p.id = P.id_base + j;
-    rs.init(P.key0, P.key1, P.step, p.id);
+// Create newborn j of the launch's step jf (CellOriginBuilder / SurfaceOriginBuilder /
+// PhasorBuilder, psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
+template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t jf,
+                                                          std::uint32_t j) {
+    const BirthGroup g = P.groups[find_group(P, P.group_begin_f[jf], P.group_begin_f[jf + 1], j)];
+    p.id = P.id_base_f[jf] + j;
+    rs.init(P.key0, P.key1, P.step + jf, p.id);
     p.tts = 0.f;
     if (g.source >= 0) {
         const std::uint32_t cell = static_cast<std::uint32_t>(g.source);
@@ -211,57 +214,71 @@ struct Lane {
     unsigned events;
     float fN, fNU;  // N/sum and (N+U)/sum of the rates of the last scattering-time draw
     bool need_target, changed, rates_ok;
+    // the measurement step the phonon is in: the step its random stream is keyed by
+    __device__ __forceinline__ std::uint32_t step() const { return rs.step; }
 };
 
 struct Outcome {
     bool alive;
     bool boundary;// reached the step boundary (a phonon-step), alive or at the last boundary
+    bool cont;    // alive, and the next step is one of this launch's
     bool tallied;
     std::uint32_t sensor;
     long long fx, fy;
 };
 
-template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive,
-                                           const float4* in_pd, const uint4* in_meta) {
+// The lane's phonon enters 'step' at its start: that step's random stream, a full step of time.
+// The same state is what a later launch would read back from the output buffer.
+__device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, std::uint32_t step) {
+    L.rs.init(P.key0, P.key1, step, L.p.id);
+    L.rem = P.dt;
+    // A phonon that scatters or draws a new scattering time in this step needs random words:
+    // make them here, where most lanes of the warp start a step together.
+    if (L.p.tts < L.rem) { L.rs.prefill(); }
+    L.need_target = true;
+    L.rates_ok = false;
+    L.events = 0;
+}
+
+template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive) {
     if (i < n_alive) {
+        const float4* in_pd = static_cast<const float4*>(P.in);
         const float4 a = in_pd[i];
-        const uint4 b = in_meta[i];
+        const uint4 b = reinterpret_cast<const uint4*>(in_pd + P.capacity)[i];
         L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
-        L.rs.init(P.key0, P.key1, P.step, L.p.id);
-        L.rem = P.dt;
-        // A phonon that scatters or draws a new scattering time in this step needs random words:
-        // make them here, where most lanes of the warp start a step together.
-        if (L.p.tts < L.rem) { L.rs.prefill(); }
+        lane_enter_step(P, L, P.step);
     } else {
-        L.rem = spawn32<S>(P, L.p, L.rs, i - n_alive);
+        const std::uint32_t k = i - n_alive;
+        std::uint32_t jf = 0;
+        while (jf + 1U < P.n_fused && k >= P.new_begin[jf + 1U]) { ++jf; }
+        L.rem = spawn32<S>(P, L.p, L.rs, jf, k - P.new_begin[jf]);// keys the stream by step P.step + jf
+        L.need_target = true;
+        L.rates_ok = false;
+        L.events = 0;
     }
     const CellF32* C = cells_of<S>(P) + meta_cell(L.p.meta);
     L.sensor = C->sensor;
     L.mat = C->material;
     L.v = vel32<S>(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
-    L.need_target = true;
-    L.rates_ok = false;
-    L.events = 0;
 }
 
 // One segment of a phonon's step: the straight flight to the next edge impact or to the end of
 // the current event (ModelSimulator::simulatePhonon / handleImpacts / nextImpact,
 // psim/src/modelSimulator.cpp:87-225).  Returns true when the phonon's step is over (it
 // reached the step boundary or was absorbed); the outcome says which.
-template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out, unsigned long long& relocations,
-                          unsigned long long& limits) {
+// The rare event-limit and collision-limit hits go straight to their global counters.
+template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out) {
     Ph32& p = L.p;
     Stream& rs = L.rs;
     const bool phasor = meta_phasor(p.meta);
     if (L.need_target) {
         if (++L.events > kMaxEventsPerStep) {// numerical corner case: end the step where the phonon is
-            ++limits;
+            atomicAdd(P.counters + 4, 1ULL);
             L.rem = 0.f;
             p.tts = fmaxf(p.tts, 0.f);
         }
         if (p.tts <= 0.f) {// time to the next scattering event (modelSimulator.cpp:148-153)
             const float3 r = rates32(materials_of<S>(P)[L.mat], sensors_of<S>(P)[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
-            const float sum = r.x + r.y + r.z;
             const float inv = __frcp_rn(r.x + r.y + r.z);
             p.tts = 1e9f * (-__logf(rs.uf())) * inv;
             L.fN = r.x * inv;
@@ -333,8 +350,8 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
             reflect(p, rs, C->spec, E);
         } else {// EmitSurface::handlePhonon (psim/src/surface.cpp:61-65)
             const EmitterDev& em = emitters_of<S>(P)[static_cast<std::uint32_t>(-(link + 2))];
-            if (P.step >= em.absorb_lo && P.step <= em.absorb_hi) {
-                out = Outcome{ false, false, false, 0U, 0, 0 };
+            if (L.step() >= em.absorb_lo && L.step() <= em.absorb_hi) {
+                out = Outcome{ false, false, false, false, 0U, 0, 0 };
                 return true;// absorbed
             }
             reflect(p, rs, C->spec, E);
@@ -351,7 +368,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
             p.py = C->vert[1].y * r1 + C->vert[2].y * r2;
             p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
             L.drifted = L.target;
-            ++relocations;
+            atomicAdd(P.counters + 1, 1ULL);
         } else {
             event_over = L.changed;
         }
@@ -363,10 +380,11 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
     p.tts -= used;
     L.need_target = true;
     if (L.rem == 0.f) {
-        const std::uint32_t next = P.step + 1U;
-        out = Outcome{ false, true, false, 0U, 0, 0 };
+        const std::uint32_t next = L.step() + 1U;
+        out = Outcome{ false, true, false, false, 0U, 0, 0 };
         if (next >= P.n_steps) { return true; }
         out.alive = true;
+        out.cont = next < P.step + P.n_fused;
         if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
             const float sv = static_cast<float>(meta_sign(p.meta)) * L.v;
             out.tallied = true;
@@ -403,10 +421,12 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
 }
 
 // Persistent lanes: each lane pulls the next phonon of the step (alive phonons first, then the
-// step's newborns) from a warp-aggregated work counter and advances it one segment per
-// iteration; a lane whose phonon finishes the step writes it out and takes the next one.  The
-// warp stays full until the step's work runs out instead of waiting for its slowest phonon.
-template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const StepParams P) {
+// steps' newborns) from a warp-aggregated work counter and advances it one segment per
+// iteration.  A phonon that crosses a boundary into another of the launch's steps stays in its
+// lane; one that leaves the launch (or dies) frees the lane for the next work item.  The warp
+// stays full until the launch's work runs out instead of waiting for its slowest phonon.
+// P is a __grid_constant__ so the per-step arrays in it are read in place with a runtime index.
+template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const __grid_constant__ StepParams P) {
     __shared__ std::uint64_t stage_bar;
     if constexpr (S) {// TMA bulk copies of the read-only tables into shared memory
         if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
@@ -432,7 +452,7 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
         }
     }
     BlockTally bt;
-    tally_init(P, bt, g_smem);
+    tally_init(P, bt, g_smem, P.n_fused);
     if constexpr (S) {
         const bool ok = mbar_wait_bounded(&stage_bar);
         if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
@@ -442,24 +462,19 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
         }
     }
     const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *P.count_clear = 0U;
-        *P.work_clear = 0U;
-        atomicMax(P.counters + 3, static_cast<unsigned long long>(n_alive) + P.n_new);
-        if (P.population != nullptr) { P.population[P.step] = n_alive + P.n_new; }
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) {
+            *P.count_clear = 0U;
+            *P.work_clear = 0U;
+        }
+        // each step's population: its newborns here, the phonons crossing into it in window_add
+        if (threadIdx.x < P.n_fused) {
+            atomicAdd(P.population + P.step + threadIdx.x, P.new_begin[threadIdx.x + 1U] - P.new_begin[threadIdx.x]);
+        }
     }
-    const std::uint32_t total = n_alive + P.n_new;
-    const std::uint32_t slot_k = P.step + 1U >= P.step_adj ? P.step + 1U - P.step_adj : 0U;
-    const float4* in_pd = static_cast<const float4*>(P.in);
-    const uint4* in_meta = reinterpret_cast<const uint4*>(in_pd + P.capacity);
-    float4* out_pd = static_cast<float4*>(P.out);
-    uint4* out_meta = reinterpret_cast<uint4*>(out_pd + P.capacity);
+    const std::uint32_t total = n_alive + P.new_begin[P.n_fused];
     const unsigned full = 0xFFFFFFFFU;
-    const unsigned lane_id = threadIdx.x & 31U;
-    const unsigned below = (1U << lane_id) - 1U;
-    unsigned long long steps = 0;
-    unsigned long long relocations = 0;
-    unsigned long long limits = 0;
+    std::uint32_t steps = 0;// phonon-steps of this thread (a launch gives each thread far fewer than 2^32)
     bool active = false;
     bool exhausted = false;// warp-uniform: the step's work counter has run out
     Lane L;
@@ -470,39 +485,57 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
             if (need != 0U) {
                 const int leader = __ffs(static_cast<int>(need)) - 1;
                 std::uint32_t base = 0;
-                if (static_cast<int>(lane_id) == leader) { base = atomicAdd(P.work, static_cast<std::uint32_t>(__popc(need))); }
+                if (static_cast<int>(threadIdx.x & 31U) == leader) { base = atomicAdd(P.work, static_cast<std::uint32_t>(__popc(need))); }
                 base = __shfl_sync(full, base, leader);
                 if (base + static_cast<std::uint32_t>(__popc(need)) >= total) { exhausted = true; }
                 if (!active) {
-                    const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & below));
+                    const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & ((1U << (threadIdx.x & 31U)) - 1U)));
                     if (i < total) {
-                        lane_start<S>(P, L, i, n_alive, in_pd, in_meta);
+                        lane_start<S>(P, L, i, n_alive);
                         active = true;
                     }
                 }
             }
         }
         if (__ballot_sync(full, active) == 0U) { break; }
-        Outcome o{ false, false, false, 0U, 0, 0 };
+        Outcome o{ false, false, false, false, 0U, 0, 0 };
         bool done = false;
-        if (active) { done = segment32<S>(P, L, o, relocations, limits); }
+        if (active) { done = segment32<S>(P, L, o); }
         const bool finishing = active && done;
-        steps += (finishing && o.boundary) ? 1ULL : 0ULL;
-        const std::uint32_t slot = reserve_slot(P, finishing && o.alive);
-        if (slot != 0xFFFFFFFFU) {
+        const bool crossing = finishing && o.alive;// into step L.step + 1
+        const bool stays = crossing && o.cont;
+        steps += (finishing && o.boundary) ? 1U : 0U;
+        const std::uint32_t slot = reserve_slot(P, crossing && !stays);
+        if (slot != 0xFFFFFFFFU) {// records: float4 {px, py, dx, dy}[capacity], then uint4 {meta, binw, tts, id}[capacity]
+            float4* out_pd = static_cast<float4*>(P.out);
             out_pd[slot] = make_float4(L.p.px, L.p.py, L.p.dx, L.p.dy);
-            out_meta[slot] = make_uint4(L.p.meta, L.p.binw, __float_as_uint(L.p.tts), L.p.id);
+            reinterpret_cast<uint4*>(out_pd + P.capacity)[slot] = make_uint4(L.p.meta, L.p.binw, __float_as_uint(L.p.tts), L.p.id);
         }
-        tally_add(P, bt, finishing && o.tallied, o.sensor, meta_sign(L.p.meta), o.fx, o.fy, slot_k);
-        if (finishing) { active = false; }
+        window_add(P, g_smem, crossing, o.tallied, L.step() - P.step, o.sensor, meta_sign(L.p.meta), o.fx, o.fy);
+        if (stays) {
+            lane_enter_step(P, L, L.step() + 1U);
+        } else if (finishing) {
+            active = false;
+        }
     }
-    block_count_add(P.counters + 0, steps);
-    block_count_add(P.counters + 1, relocations);
-    block_count_add(P.counters + 4, limits);
-    tally_flush(P, bt, slot_k);
+    block_count_add(P.counters + 0, static_cast<unsigned long long>(steps));
+    window_flush(P, g_smem);
 }
 
 }// namespace
+
+// Largest population of the run (counters[3]) from the per-step populations.
+__global__ void population_max_kernel(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters) {
+    unsigned m = 0U;
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) { m = max(m, population[i]); }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) { m = max(m, __shfl_down_sync(0xFFFFFFFFU, m, o)); }
+    if ((threadIdx.x & 31U) == 0U && m != 0U) { atomicMax(counters + 3, static_cast<unsigned long long>(m)); }
+}
+
+void launch_population_max(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters, cudaStream_t stream) {
+    population_max_kernel<<<1, 1024, 0, stream>>>(population, n, counters);
+}
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
     if (P.stage_mask != 0U) {

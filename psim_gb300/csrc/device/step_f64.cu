@@ -84,7 +84,7 @@ __device__ __forceinline__ void sample_freq(const StepParams& P, Ph64& p, Stream
 }
 
 __device__ double spawn64(const StepParams& P, Ph64& p, Stream& rs, std::uint32_t j) {
-    const BirthGroup g = P.groups[find_group(P, j)];
+    const BirthGroup g = P.groups[find_group(P, P.group_begin, P.group_end, j)];
     p.id = P.id_base + j;
     rs.init(P.key0, P.key1, P.step, p.id);
     p.tts = 0.;
@@ -287,7 +287,7 @@ __device__ Outcome transport64(const StepParams& P, Ph64& p, Stream& rs, double 
 __global__ void __launch_bounds__(kBlock) step_kernel_f64(const StepParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     BlockTally bt;
-    tally_init(P, bt, smem);
+    tally_init(P, bt, smem, 1U);
     const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         *P.count_clear = 0U;

@@ -19,10 +19,9 @@ __device__ __forceinline__ std::uint32_t alias_draw(const std::uint32_t* table, 
     return min(o, static_cast<std::uint32_t>(2 * kBins - 1));// columns >= 2000 carry no probability
 }
 
-// Newborn j of this step -> its birth group (groups sorted by 'first').
-__device__ __forceinline__ std::uint32_t find_group(const StepParams& P, std::uint32_t j) {
-    std::uint32_t lo = P.group_begin;
-    std::uint32_t hi = P.group_end;// groups[lo].first <= j < groups[hi].first (hi exclusive)
+// Newborn j of a step -> its birth group among groups [lo, hi) of that step (sorted by 'first').
+__device__ __forceinline__ std::uint32_t find_group(const StepParams& P, std::uint32_t lo, std::uint32_t hi, std::uint32_t j) {
+    // invariant: groups[lo].first <= j < groups[hi].first (hi exclusive)
     while (hi - lo > 1) {
         const std::uint32_t mid = (lo + hi) >> 1;
         if (__ldg(&P.groups[mid].first) <= j) {
@@ -34,12 +33,17 @@ __device__ __forceinline__ std::uint32_t find_group(const StepParams& P, std::ui
     return lo;
 }
 
-// Shared-memory tally of one block for the boundary this step ends on.
+// Shared-memory tally of one block: one slot of S sensors per boundary the launch ends steps on
+// (slot j: the boundary after step P.step + j), plus the phonons crossing each boundary alive.
+// Layout from 'base': fx[n], fy[n] (8-byte aligned), count[n], cross[kMaxFused], n = slots x S.
 struct BlockTally {
-    int* count;
-    long long* fx;
-    long long* fy;
+    unsigned char* base;
+    std::uint32_t n;
     bool shared;
+    __device__ __forceinline__ long long* fx() const { return reinterpret_cast<long long*>(base); }
+    __device__ __forceinline__ long long* fy() const { return fx() + n; }
+    __device__ __forceinline__ int* count() const { return reinterpret_cast<int*>(fy() + n); }
+    __device__ __forceinline__ unsigned* cross() const { return reinterpret_cast<unsigned*>(count() + n); }
 };
 
 __device__ __forceinline__ void tally_add(const StepParams& P, BlockTally& bt, bool tallied, std::uint32_t sensor,
@@ -52,9 +56,9 @@ __device__ __forceinline__ void tally_add(const StepParams& P, BlockTally& bt, b
     const int leader = __ffs(static_cast<int>(peers)) - 1;
     const int c = __reduce_add_sync(peers, sign);
     if (bt.shared) {
-        if (lane == leader) { atomicAdd(bt.count + sensor, c); }
-        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx + sensor), static_cast<unsigned long long>(fx));
-        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy + sensor), static_cast<unsigned long long>(fy));
+        if (lane == leader) { atomicAdd(bt.count() + sensor, c); }
+        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx() + sensor), static_cast<unsigned long long>(fx));
+        atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy() + sensor), static_cast<unsigned long long>(fy));
     } else {
         TallySlot* t = P.tally + static_cast<std::size_t>(slot) * P.n_sensors + sensor;
         if (lane == leader) { atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(c))); }
@@ -102,13 +106,75 @@ __device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar) {
     return false;
 }
 
+// The tally of an FP32 launch (one slot per covered step), rebuilt from the parameters where it
+// is used so that no pointer to it stays live in registers.
+__device__ __forceinline__ BlockTally window_tally(const StepParams& P, unsigned char* smem) {
+    return BlockTally{ smem + P.off_tally, P.n_fused * P.n_sensors, P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors) };
+}
+
+// FP32 launch over several steps: a phonon ending step P.step + j at its boundary.  'crossing'
+// phonons go on into the next step (they count towards its population); 'tallied' ones (the
+// boundary is recorded) add their sign and flux to sensor 'sensor' of slot j.  Each lane adds its
+// own: at a few crossings per warp and iteration spread over the sensors, plain shared-memory
+// atomics cost less than grouping the lanes first (__match_any_sync every iteration).
+// 'smem' is the kernel's dynamic shared memory; the tally sits at P.off_tally in it.
+__device__ __forceinline__ void window_add(const StepParams& P, unsigned char* smem, bool crossing, bool tallied, std::uint32_t j,
+                                           std::uint32_t sensor, int sign, long long fx, long long fy) {
+    if (!crossing) { return; }
+    const BlockTally bt = window_tally(P, smem);
+    if (bt.shared) {
+        const std::uint32_t i = j * P.n_sensors + sensor;
+        atomicAdd(bt.cross() + j, 1U);
+        if (tallied) {
+            atomicAdd(bt.count() + i, sign);
+            atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx() + i), static_cast<unsigned long long>(fx));
+            atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy() + i), static_cast<unsigned long long>(fy));
+        }
+    } else {
+        atomicAdd(P.population + P.step + j + 1U, 1U);
+        if (tallied) {
+            TallySlot* t = P.tally + static_cast<std::size_t>(P.step + j + 1U - P.step_adj) * P.n_sensors + sensor;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(sign)));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fx), static_cast<unsigned long long>(fx));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fy), static_cast<unsigned long long>(fy));
+        }
+    }
+}
+
+// Adds a block's window tally to the run's tallies (recorded boundaries only) and its crossing
+// counts to the population of the steps they enter.
+__device__ __forceinline__ void window_flush(const StepParams& P, unsigned char* smem) {
+    const BlockTally bt = window_tally(P, smem);
+    if (!bt.shared) { return; }
+    __syncthreads();
+    const std::uint32_t n = P.n_fused * P.n_sensors;
+    for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const std::uint32_t j = i / P.n_sensors;
+        const std::uint32_t s = i - j * P.n_sensors;
+        const std::uint32_t boundary = P.step + j + 1U;
+        if (boundary < P.step_adj || boundary - P.step_adj >= P.n_recorded) { continue; }
+        const int c = bt.count()[i];
+        const long long fx = bt.fx()[i];
+        const long long fy = bt.fy()[i];
+        if (c != 0 || fx != 0 || fy != 0) {
+            TallySlot* t = P.tally + static_cast<std::size_t>(boundary - P.step_adj) * P.n_sensors + s;
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(c)));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fx), static_cast<unsigned long long>(fx));
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t->fy), static_cast<unsigned long long>(fy));
+        }
+    }
+    if (threadIdx.x < P.n_fused && P.step + threadIdx.x + 1U < P.n_steps && bt.cross()[threadIdx.x] != 0U) {
+        atomicAdd(P.population + P.step + threadIdx.x + 1U, bt.cross()[threadIdx.x]);
+    }
+}
+
 __device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt, std::uint32_t slot) {
     if (!bt.shared) { return; }
     __syncthreads();
     for (std::uint32_t s = threadIdx.x; s < P.n_sensors; s += blockDim.x) {
-        const int c = bt.count[s];
-        const long long fx = bt.fx[s];
-        const long long fy = bt.fy[s];
+        const int c = bt.count()[s];
+        const long long fx = bt.fx()[s];
+        const long long fy = bt.fy()[s];
         if (c != 0 || fx != 0 || fy != 0) {
             TallySlot* t = P.tally + static_cast<std::size_t>(slot) * P.n_sensors + s;
             atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(c)));
@@ -118,25 +184,29 @@ __device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt,
     }
 }
 
-__device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, unsigned char* smem) {
-    // layout: fx[S], fy[S] (8-byte aligned), count[S]; S <= kSharedSensors
+__device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, unsigned char* smem, std::uint32_t slots) {
+    // layout: fx[slots*S], fy[slots*S] (8-byte aligned), count[slots*S], cross[kMaxFused];
+    // S <= kSharedSensors
     bt.shared = P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors);
-    bt.fx = reinterpret_cast<long long*>(smem + P.off_tally);
-    bt.fy = bt.fx + P.n_sensors;
-    bt.count = reinterpret_cast<int*>(bt.fy + P.n_sensors);
+    const std::uint32_t n = slots * P.n_sensors;
+    bt.base = smem + P.off_tally;
+    bt.n = n;
     if (bt.shared) {
-        for (std::uint32_t s = threadIdx.x; s < P.n_sensors; s += blockDim.x) {
-            bt.fx[s] = 0;
-            bt.fy[s] = 0;
-            bt.count[s] = 0;
+        for (std::uint32_t s = threadIdx.x; s < n; s += blockDim.x) {
+            bt.fx()[s] = 0;
+            bt.fy()[s] = 0;
+            bt.count()[s] = 0;
         }
+        if (threadIdx.x < kMaxFused) { bt.cross()[threadIdx.x] = 0U; }
     }
     __syncthreads();
 }
 
-// Shared bytes of a block's tally for S sensors (0 when S exceeds kSharedSensors), 16-aligned.
-inline std::size_t tally_smem_bytes(std::uint32_t S) {
-    return S <= static_cast<std::uint32_t>(kSharedSensors) ? ((static_cast<std::size_t>(S) * 20 + 15) / 16) * 16 : 0;
+// Shared bytes of a block's tally with 'slots' boundary slots of S sensors (0 when S exceeds
+// kSharedSensors: the tallies then go straight to global memory), 16-aligned.
+inline std::size_t tally_smem_bytes(std::uint32_t S, std::uint32_t slots = 1) {
+    if (S > static_cast<std::uint32_t>(kSharedSensors)) { return 0; }
+    return ((static_cast<std::size_t>(S) * slots * 20 + kMaxFused * 4 + 15) / 16) * 16;
 }
 
 // Warp-aggregated slot reservation in the output buffer; returns the slot or UINT32_MAX.

@@ -55,13 +55,42 @@ def test_launch_shape_does_not_change_results(api, monkeypatch):
     assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
 
 
+@pytest.mark.parametrize("name", ["kinked_small", "plate_small", "bar_ss"])
+def test_steps_per_launch_do_not_change_results(api, monkeypatch, name):
+    """An FP32 launch covers up to 8 measurement steps and carries phonons across the inner
+    boundaries in registers.  Tallies, the population history and the phonon-step count equal
+    those of one step per launch, with shared-memory tables and with global ones."""
+    ref = None
+    for stage, fuse in (("1", "1"), ("1", "3"), ("1", "8"), ("0", "5")):
+        monkeypatch.setenv("PSIM_GB300_STAGE", stage)
+        monkeypatch.setenv("PSIM_GB300_FUSE", fuse)
+        m = api.Model(model_path(name))
+        m.run(seed=11)
+        e, f = m.tallies()
+        c = m.counters()
+        got = (e, f, m.population(), c["phonon_steps"], c["max_population"])
+        assert c["steps_per_launch"] == int(fuse)
+        assert c["transport_launches"] == -(-m.n_steps // int(fuse))
+        if ref is None:
+            ref = got
+            continue
+        assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1]), (stage, fuse)
+        assert np.array_equal(ref[2], got[2]), (stage, fuse)
+        assert ref[3:] == got[3:], (stage, fuse)
+    monkeypatch.delenv("PSIM_GB300_STAGE")
+    monkeypatch.delenv("PSIM_GB300_FUSE")
+
+
 def test_counters_and_phonon_steps(api):
     m = api.Model(model_path("bar_ss"))
     m.run(seed=3)
     c = m.counters()
     assert c["phonons"] > 90000
     assert c["phonon_steps"] > c["phonons"]
-    assert c["kernel_launches"] >= 1000
+    # 1000 steps: ceil(1000 / steps per launch) transport launches and one population pass
+    assert 1 <= c["steps_per_launch"] <= 8
+    assert c["transport_launches"] == -(-1000 // c["steps_per_launch"])
+    assert c["kernel_launches"] == c["transport_launches"] + 1
     assert c["max_population"] > 0
     assert c["kernel_ms"] > 0
     # SS records the last 10 % of steps: every tallied phonon-step adds its sign; the net
