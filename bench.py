@@ -267,6 +267,12 @@ def main():
         roofline["traffic"] = tr.get("dram_bytes_per_phonon_step", 0) * phonon_steps / transport_launches
         roofline["traffic_source"] = tr.get("source")
 
+    # time to steady state of the last timed run (a cold start: every cell at T_ref), by the
+    # detector on its device tallies; outside the timed region
+    onset, _ = model.steady_state(window=250, batches=5, z=3.0, patience=3)
+    steady = {"onset_step": onset, "onset_ns": onset * args.dt_ps * 1e-3 if onset >= 0 else None,
+              "criterion": "windows of 250 steps (5 batch means) agree within 3 SE for 3 windows, energy and flux, every sensor"}
+
     # ---- e2e through the public C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -315,7 +321,7 @@ def main():
                        "precision": args.precision, "bench_step": "one full simulation run",
                        "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
-            "clocks": clk, "wall_s_timed": wall,
+            "clocks": clk, "wall_s_timed": wall, "steady_state": steady,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -113,6 +113,18 @@ SIGNATURES = {
     "psim_final_temps_noalloc": (ctypes.c_int, [ctypes.POINTER(InterpDesc), ctypes.c_void_p, ctypes.c_uint64,
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "psim_final_temps_noalloc_max_bytes": (ctypes.c_uint64, []),
+    "psim_steady_state": (ctypes.c_int, [_c_i64p, _c_dp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_double, ctypes.c_uint32, _c_i64p, _c_i64p]),
+    "psim_sim_steady_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_uint32,
+                                             _c_i64p, _c_i64p]),
+    "psim_model_steady_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
+                                               ctypes.c_uint32, _c_i64p, _c_i64p]),
+    "psim_model_set_steady_stop": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
+                                                  ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64]),
+    "psim_sim_set_steady_stop": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
+                                                ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64]),
+    "psim_model_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
+    "psim_sim_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
     "psim_geom_intersect": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
@@ -170,6 +182,9 @@ class Model:
         self._h = ctypes.c_void_p()
         _check(lib().psim_model_load_json(json_path.encode(), ctypes.byref(self._h)))
         self.path = json_path
+        self._shape()
+
+    def _shape(self) -> None:
         s, k, c, n, r = (ctypes.c_int64() for _ in range(5))
         _check(lib().psim_model_shape(self._h, ctypes.byref(s), ctypes.byref(k), ctypes.byref(c), ctypes.byref(n),
                                       ctypes.byref(r)))
@@ -196,7 +211,18 @@ class Model:
     def run(self, seed: int = 1, precision: int = FP32, stream: Optional[int] = None) -> "Model":
         _check(lib().psim_model_set_options(self._h, seed, precision, ctypes.c_void_p(stream or 0)))
         _check(lib().psim_model_run(self._h))
+        self._shape()  # a run stopped at steady state records fewer steps
         return self
+
+    def set_steady_stop(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3, check_every: int = 0,
+                        enable: bool = True) -> None:
+        """Stop later runs at steady state (single-run periodic or transient models)."""
+        _check(lib().psim_model_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, check_every))
+
+    def steps_run(self) -> int:
+        out = ctypes.c_uint64()
+        _check(lib().psim_model_steps_run(self._h, ctypes.byref(out)))
+        return int(out.value)
 
     def measurements(self) -> np.ndarray:
         """[S, 6]: T, SE(T), flux x, SE, flux y, SE averaged over runs."""
@@ -234,6 +260,10 @@ class Model:
         d = SimDesc()
         _check(lib().psim_model_sim_desc(self._h, ctypes.byref(d)))
         return d
+
+    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3) -> Tuple[int, np.ndarray]:
+        """Steady-state onset (step, -1 if none) and per-sensor onsets over the last run."""
+        return _steady(lib().psim_model_steady_state, self._h, self.n_sensors, window, batches, z, patience)
 
     def interp_desc(self, eff_energy: float = 0.0) -> InterpDesc:
         d = InterpDesc()
@@ -291,6 +321,18 @@ class Simulator:
         _check(lib().psim_sim_tallies(self._h, _i64(energy), _dp(flux)))
         return energy, flux
 
+    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3) -> Tuple[int, np.ndarray]:
+        return _steady(lib().psim_sim_steady_state, self._h, self.desc.n_sensors, window, batches, z, patience)
+
+    def set_steady_stop(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3, check_every: int = 0,
+                        enable: bool = True) -> None:
+        _check(lib().psim_sim_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, check_every))
+
+    def steps_run(self) -> int:
+        out = ctypes.c_uint64()
+        _check(lib().psim_sim_steps_run(self._h, ctypes.byref(out)))
+        return int(out.value)
+
     def counters(self) -> dict:
         c = RunCounters()
         _check(lib().psim_sim_counters(self._h, ctypes.byref(c)))
@@ -312,6 +354,27 @@ def interpret(desc: InterpDesc, energy: np.ndarray, flux: np.ndarray):
     stats = np.zeros((S, 6))
     _check(lib().psim_interpret(ctypes.byref(desc), _i64(energy), _dp(flux), _dp(temps), _dp(fluxes), _dp(stats)))
     return temps, fluxes, stats
+
+
+def _steady(fn, handle, n_sensors: int, window: int, batches: int, z: float, patience: int) -> Tuple[int, np.ndarray]:
+    onset = ctypes.c_int64()
+    per = np.zeros(n_sensors, dtype=np.int64)
+    _check(fn(handle, window, batches, z, patience, ctypes.byref(onset), _i64(per)))
+    return int(onset.value), per
+
+
+def steady_state(energy: np.ndarray, flux: np.ndarray, window: int = 250, batches: int = 5, z: float = 3.0,
+                 patience: int = 3) -> Tuple[int, np.ndarray]:
+    """psim_steady_state on raw tallies energy [S,K] and flux [S,K,2]: (onset step or -1, per-sensor onsets)."""
+    energy = np.ascontiguousarray(energy, dtype=np.int64)
+    flux = np.ascontiguousarray(flux, dtype=np.float64)
+    S, K = energy.shape
+    assert flux.shape == (S, K, 2)
+    onset = ctypes.c_int64()
+    per = np.zeros(S, dtype=np.int64)
+    _check(lib().psim_steady_state(_i64(energy), _dp(flux), S, K, window, batches, z, patience, ctypes.byref(onset),
+                                   _i64(per)))
+    return int(onset.value), per
 
 
 def final_temps(desc: InterpDesc, energy: np.ndarray, start_step: int) -> np.ndarray:

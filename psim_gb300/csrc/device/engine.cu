@@ -621,13 +621,13 @@ void Engine::run(int precision, void* stream_ptr) {
     last_stage_mask_ = P.stage_mask;
     if (const char* g = std::getenv("PSIM_GB300_GRID"); g != nullptr && std::atoi(g) > 0) { grid = std::atoi(g); }// launch-shape override
 
-    // FP32: launch w covers steps [s0, s0 + tw); FP64: one step per launch.
+    // FP32: launch w covers steps [s0, s0 + tw); FP64: one step per launch.  Steps [from, to) are
+    // enqueued; the launch index w (which buffer and counter each launch uses) runs on across calls.
     std::uint64_t launches = 0;
-    auto enqueue = [&]() {
-        launches = 0;
-        std::uint64_t w = 0;
-        for (std::uint64_t s0 = 0; s0 < d.steps; ++w) {
-            std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, d.steps - s0));
+    std::uint64_t w = 0;
+    auto enqueue = [&](std::uint64_t from, std::uint64_t to) {
+        for (std::uint64_t s0 = from; s0 < to; ++w) {
+            std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, to - s0));
             // every work item of a launch is numbered in 32 bits
             auto items = [&](std::uint32_t n) {
                 std::uint64_t t = P.capacity;
@@ -664,18 +664,45 @@ void Engine::run(int precision, void* stream_ptr) {
             ++launches;
             s0 += tw;
         }
+    };
+    auto finish = [&](std::uint64_t steps_done) {
         if (!fp64) {
-            launch_population_max(P.population, static_cast<std::uint32_t>(d.steps), P.counters, stream);
+            launch_population_max(P.population, static_cast<std::uint32_t>(steps_done), P.counters, stream);
             ++launches;
         }
     };
+    std::uint64_t checks = 0;
+    steps_run_ = d.steps;
 
     check(cudaEventRecord(I.ev0, stream), "event record");
-    if (use_graph_) {
+    if (stop_on_) {// launches in chunks, the recorded steps checked for steady state after each
+        if (d.step_adj != 0 || d.recorded != d.steps) {
+            throw std::invalid_argument("stopping at steady state needs every step recorded (periodic or transient runs)");
+        }
+        const std::uint64_t min_steps = static_cast<std::uint64_t>(stop_crit_.patience + 1) * stop_crit_.window;
+        const std::uint64_t every = stop_check_ > 0 ? stop_check_ : min_steps;
+        std::uint64_t done = 0;
+        while (done < d.steps) {
+            const std::uint64_t to = std::min<std::uint64_t>(d.steps, done + every);
+            enqueue(done, to);
+            check(cudaGetLastError(), "step launch");
+            done = to;
+            if (done < d.steps && done >= min_steps) {
+                ++checks;
+                if (steady_onset_device(I.tally.p, d.n_sensors, done, stop_crit_, nullptr, stream) >= 0) { break; }
+            }
+        }
+        steps_run_ = done;
+        finish(done);
+        check(cudaGetLastError(), "step launch");
+        check(cudaEventRecord(I.ev1, stream), "event record");
+        check(cudaStreamSynchronize(stream), "run sync");
+    } else if (use_graph_) {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        enqueue();
+        enqueue(0, d.steps);
+        finish(d.steps);
         check(cudaStreamEndCapture(stream, &graph), "end capture");
         check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
         check(cudaGraphLaunch(exec, stream), "graph launch");
@@ -684,7 +711,8 @@ void Engine::run(int precision, void* stream_ptr) {
         cudaGraphExecDestroy(exec);
         cudaGraphDestroy(graph);
     } else {
-        enqueue();
+        enqueue(0, d.steps);
+        finish(d.steps);
         check(cudaGetLastError(), "step launch");
         check(cudaEventRecord(I.ev1, stream), "event record");
         check(cudaStreamSynchronize(stream), "run sync");
@@ -701,12 +729,19 @@ void Engine::run(int precision, void* stream_ptr) {
     counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
     counters_.kernel_ms += ms;
     counters_.d2h_bytes += sizeof c;
-    counters_.kernel_launches += launches;
+    counters_.kernel_launches += launches + checks;
     counters_.transport_launches += fp64 ? launches : launches - 1;// FP32 adds one population pass
     counters_.steps_per_launch = fused;
     last_fused_ = fused;
     I.builders_ready = false;
     if (c[2] != 0) { throw std::length_error("phonon buffer overflow: the device ran out of memory for the population"); }
+}
+
+void Engine::set_steady_stop(bool on, const SteadyCriterion& c, std::uint64_t check_every) {
+    if (on) { validate_steady(c); }
+    stop_on_ = on;
+    stop_crit_ = c;
+    stop_check_ = check_every;
 }
 
 void Engine::reset() {
@@ -718,15 +753,17 @@ void Engine::reset() {
 }
 
 namespace {
-void unpack(const Engine& eng, Buf& e, Buf& f, cudaStream_t stream, const void* tally) {
+// The first K recorded steps of the tallies, [K][S] records -> energy[S][K], flux[S][K][2].
+void unpack(const Engine& eng, Buf& e, Buf& f, cudaStream_t stream, const void* tally, std::uint64_t K) {
     const SimDesc& d = eng.desc();
-    const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
+    if (K > d.recorded) { throw std::invalid_argument("more steps asked for than recorded"); }
+    const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * K;
     if (e.bytes < SK * sizeof(long long) || e.p == nullptr) { e.alloc(SK * sizeof(long long)); }
     if (f.bytes < SK * 2 * sizeof(double) || f.p == nullptr) { f.alloc(SK * 2 * sizeof(double)); }
     if (SK > 0) {
         const int blocks = static_cast<int>(std::min<std::uint64_t>((SK + 255) / 256, 8192));
-        unpack_kernel<<<blocks, 256, 0, stream>>>(static_cast<const TallySlot*>(tally), d.n_sensors, d.recorded,
-                                                 e.as<long long>(), f.as<double>());
+        unpack_kernel<<<blocks, 256, 0, stream>>>(static_cast<const TallySlot*>(tally), d.n_sensors, K, e.as<long long>(),
+                                                 f.as<double>());
         check(cudaGetLastError(), "unpack kernel");
     }
 }
@@ -738,10 +775,11 @@ void Engine::population(std::uint32_t* out) const {
     counters_.d2h_bytes += desc_.steps * sizeof(std::uint32_t);
 }
 
-void Engine::tallies(std::int64_t* energy, double* flux) const {
+void Engine::tallies(std::int64_t* energy, double* flux, std::uint64_t K) const {
     Impl& I = *impl_;
-    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
-    const std::uint64_t SK = static_cast<std::uint64_t>(desc_.n_sensors) * desc_.recorded;
+    K = std::min<std::uint64_t>(K, desc_.recorded);
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p, K);
+    const std::uint64_t SK = static_cast<std::uint64_t>(desc_.n_sensors) * K;
     if (energy != nullptr) {
         check(cudaMemcpyAsync(energy, I.unpacked_energy.p, SK * sizeof(long long), cudaMemcpyDeviceToHost, I.own), "copy energy");
         counters_.d2h_bytes += SK * sizeof(long long);
@@ -755,7 +793,7 @@ void Engine::tallies(std::int64_t* energy, double* flux) const {
 
 void Engine::interpret(const InterpDesc& d, double* temps, double* fluxes, double* stats) const {
     Impl& I = *impl_;
-    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p, d.recorded);
     interpret_device(d, I.unpacked_energy.as<long long>(), I.unpacked_flux.as<double>(), temps, fluxes, stats, I.own);
     const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
     counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
@@ -763,9 +801,17 @@ void Engine::interpret(const InterpDesc& d, double* temps, double* fluxes, doubl
     counters_.d2h_bytes += (temps != nullptr ? SK * 8 : 0) + (fluxes != nullptr ? SK * 16 : 0) + (stats != nullptr ? d.n_sensors * 48ULL : 0);
 }
 
+long long Engine::steady_onset(const SteadyCriterion& c, long long* per_sensor) const {
+    Impl& I = *impl_;
+    const long long onset = steady_onset_device(I.tally.p, desc_.n_sensors, std::min<std::uint64_t>(desc_.recorded, steps_run_), c,
+                                                per_sensor, I.own);
+    counters_.d2h_bytes += desc_.n_sensors * 8ULL;
+    return onset;
+}
+
 void Engine::final_temps(const InterpDesc& d, std::uint64_t start, double* out) const {
     Impl& I = *impl_;
-    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p);
+    unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p, d.recorded);
     final_temps_device(d, I.unpacked_energy.as<long long>(), start, out, I.own);
     counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
                            + d.material.size() * 4 + d.mat_temp_begin.size() * 8;

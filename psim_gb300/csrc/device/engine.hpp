@@ -71,6 +71,14 @@ struct InterpDesc {
     std::vector<double> temps, energies;
 };
 
+// Steady-state criterion over windows of recorded steps (device/steady.cu).
+struct SteadyCriterion {
+    std::uint32_t window{ 250 }; // steps per window
+    std::uint32_t batches{ 5 };  // batch means per window (window is a multiple of it)
+    double z{ 3. };              // agreement tolerance in combined standard errors
+    std::uint32_t patience{ 3 }; // consecutive agreeing windows
+};
+
 class Engine {
 public:
     explicit Engine(const SimDesc& desc);
@@ -95,11 +103,20 @@ public:
 
     // Phonons in flight at each measurement step of the last run (alive + born), [steps].
     void population(std::uint32_t* out) const;
-    // Raw tallies (host): energy[S][K], flux[S][K][2].
-    void tallies(std::int64_t* energy, double* flux) const;
+    // Raw tallies (host) of the first K recorded steps (all of them by default): energy[S][K],
+    // flux[S][K][2].
+    void tallies(std::int64_t* energy, double* flux, std::uint64_t K = UINT64_MAX) const;
     // Device-resident interpretation of the current tallies.
     void interpret(const InterpDesc& d, double* temps, double* fluxes, double* stats) const;
     void final_temps(const InterpDesc& d, std::uint64_t start, double* out) const;
+    // Steady-state onset over the last run's recorded steps (-1: not steady).
+    long long steady_onset(const SteadyCriterion& c, long long* per_sensor) const;
+    // Stop runs once the recorded steps are steady, checked every check_every steps (rounded up
+    // to whole launches; 0 = every patience x window steps).  Needs every step recorded
+    // (periodic or transient); run() throws otherwise.
+    void set_steady_stop(bool on, const SteadyCriterion& c, std::uint64_t check_every);
+    // Measurement steps the last run simulated (all of them unless it stopped at steady state).
+    std::uint64_t steps_run() const noexcept { return steps_run_; }
 
     const RunCounters& counters() const noexcept { return counters_; }
     // bytes copied host->device when the model was created (geometry, tables, materials)
@@ -119,8 +136,21 @@ private:
     bool stage_tables_{ true };
     std::uint32_t last_stage_mask_{ 0 };
     std::uint32_t last_fused_{ 1 };
+    bool stop_on_{ false };
+    SteadyCriterion stop_crit_{};
+    std::uint64_t stop_check_{ 0 };
+    std::uint64_t steps_run_{ 0 };
     int grid_override_{ 0 };
 };
+
+void validate_steady(const SteadyCriterion& c);
+// Onset step of steady state over the first k_used recorded steps of device tallies [K][S]
+// (TallySlot records), or -1; per_sensor[S] (may be null) gets each sensor's onset.
+long long steady_onset_device(const void* tally, std::uint32_t S, std::uint64_t k_used, const SteadyCriterion& c,
+                              long long* per_sensor, void* stream);
+// The same on host tallies energy[S][K], flux[S][K][2].
+long long steady_onset_host(const std::int64_t* energy, const double* flux, std::uint32_t S, std::uint64_t K,
+                            const SteadyCriterion& c, long long* per_sensor);
 
 // Stand-alone interpreter on host arrays (psim_interpret / psim_final_temps).
 void interpret_host(const InterpDesc& d, const std::int64_t* energy, const double* flux, double* temps, double* fluxes,

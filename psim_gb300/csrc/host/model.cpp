@@ -498,7 +498,11 @@ gpu::InterpDesc HostModel::interp_desc(double eff) const {
 // it before the results are scaled (model.cpp:171); with MAX_ITERS = 1 no re-run follows.
 void HostModel::run() {
     const auto t0 = std::chrono::steady_clock::now();
+    if (stop_on_ && (num_runs_ != 1 || type_ == SimType::SteadyState)) {
+        throw std::invalid_argument("stopping at steady state needs a single-run periodic or transient model");
+    }
     runs_.clear();
+    recorded_ = desc_.recorded;
     for (std::size_t run = 0; run < num_runs_; ++run) {
         const auto [mn, mx] = bounds();
         build_tables(mn, mx);
@@ -512,7 +516,9 @@ void HostModel::run() {
         const std::vector<double> sensor_t0 = sensor_init_temps();
         const std::uint64_t run_seed = seed_ * 0x9E3779B97F4A7C15ULL + run * 0xD1B54A32D192ED03ULL + 1;
         engine_->init_builders(t_eq_, eff_energy_, cell_energy.data(), emit_energy.data(), sensor_t0.data(), run_seed);
+        engine_->set_steady_stop(stop_on_, stop_crit_, stop_check_);
         engine_->run(precision_, stream_);
+        recorded_ = std::min<std::size_t>(desc_.recorded, engine_->steps_run());
         if (type_ == SimType::SteadyState) {
             std::vector<double> finals(sensors_.size());
             engine_->final_temps(interp_desc(eff_energy_), start_step_, finals.data());
@@ -577,7 +583,7 @@ std::vector<std::array<double, 6>> HostModel::averaged() const {// OutputManager
 
 void HostModel::tallies(std::int64_t* energy, double* flux) const {
     if (!engine_) { throw std::runtime_error("the model has not been run"); }
-    engine_->tallies(energy, flux);
+    engine_->tallies(energy, flux, recorded_);
 }
 
 const gpu::RunCounters& HostModel::counters() const {

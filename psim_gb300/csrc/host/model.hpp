@@ -78,11 +78,20 @@ public:
         precision_ = precision;
         stream_ = stream;
     }
+    // Stop each run once its recorded steps are steady (single-run periodic or transient models).
+    void set_steady_stop(bool on, const gpu::SteadyCriterion& c, std::uint64_t check_every) {
+        if (on) { gpu::validate_steady(c); }
+        stop_on_ = on;
+        stop_crit_ = c;
+        stop_check_ = check_every;
+    }
     void run();// Model::runSimulation
     void export_results(const std::string& json_path, double seconds) const;
 
     std::size_t n_sensors() const noexcept { return sensors_.size(); }
     std::size_t n_cells() const noexcept { return cells_.size(); }
+    // Recorded steps of the results: all the model records, or those simulated before a stop at
+    // steady state.
     std::size_t n_recorded() const noexcept { return recorded_; }
     std::size_t n_steps() const noexcept { return steps_; }
     std::size_t n_runs() const noexcept { return num_runs_; }
@@ -126,6 +135,9 @@ private:
     std::uint64_t seed_{ 1 };
     int precision_{ 0 };
     void* stream_{ nullptr };
+    bool stop_on_{ false };
+    gpu::SteadyCriterion stop_crit_{};
+    std::uint64_t stop_check_{ 0 };
 
     gpu::SimDesc desc_;
     std::unique_ptr<gpu::Engine> engine_;
