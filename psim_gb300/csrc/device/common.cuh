@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #include <cuda_runtime.h>
 
@@ -144,18 +145,25 @@ struct Stream {
 // FP32 cell record, 128 bytes (one cache line).  Local frame: origin at the cell's first
 // vertex.  For edge e (vertices e -> e+1): outward unit normal (nx, ny) and offset h, so a
 // point p is inside the edge's half-plane when nx*px + ny*py < h.
+// 112 bytes = 28 words: successive records start 4 banks apart, so the lanes of a warp reading
+// the same field of different cells from shared memory spread over 8 bank groups (a 128-byte
+// record would put every cell's field in the same banks).
 struct alignas(16) CellF32 {
-    float4 edge[3];      // nx, ny, h, length
-    float2 vert[3];      // local vertices (vert[0] = 0,0)
+    float4 edge[3];      // nx, ny, h; w: the edge's link as int bits (>= 0 neighbour cell, -1 boundary,
+                         // <= -2 emitter -(link+2))
+    float2 v1, v2;       // local vertices 1 and 2 (vertex 0 is the origin)
     float2 offset[3];    // add to a local position when crossing edge e into the neighbour
-    int link[3];         // >= 0 neighbour cell, -1 boundary, <= -2 emitter -(link+2)
     std::uint32_t rev;   // neighbour's entry edge per edge (2 bits each); bit 8+e: flip backscatter normal
     std::uint32_t sensor;
     float spec;
     std::uint32_t material;
-    std::uint32_t pad;
 };
-static_assert(sizeof(CellF32) == 128, "CellF32 must be one 128-byte line");
+static_assert(sizeof(CellF32) == 112, "CellF32 is 112 bytes (28 words)");
+__host__ __device__ __forceinline__ int edge_link(const float4& e) {
+    int v;
+    std::memcpy(&v, &e.w, sizeof v);
+    return v;
+}
 
 // FP64 cell record: the three edge lines in the reference's Line form and the triangle.
 struct Line64 {

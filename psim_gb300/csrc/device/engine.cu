@@ -164,7 +164,9 @@ void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF6
         for (int e = 0; e < 3; ++e) {
             const psim::P2 a = vtx(c, e);
             const psim::P2 b = vtx(c, (e + 1) % 3);
-            f.vert[e] = make_float2(static_cast<float>(a.x - o.x), static_cast<float>(a.y - o.y));
+            const float2 local = make_float2(static_cast<float>(a.x - o.x), static_cast<float>(a.y - o.y));
+            if (e == 1) { f.v1 = local; }
+            if (e == 2) { f.v2 = local; }
             g.vx[e] = a.x;
             g.vy[e] = a.y;
             g.edge[e] = line64(a, b);
@@ -172,8 +174,7 @@ void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF6
             g.nx[e] = n_in.x;
             g.ny[e] = n_in.y;
             const double h = -(n_in.x * (a.x - o.x) + n_in.y * (a.y - o.y));
-            f.edge[e] = make_float4(static_cast<float>(-n_in.x), static_cast<float>(-n_in.y), static_cast<float>(h),
-                                    static_cast<float>(psim::dist2(a, b)));
+            f.edge[e] = make_float4(static_cast<float>(-n_in.x), static_cast<float>(-n_in.y), static_cast<float>(h), 0.f);// w: link, below
             const std::uint32_t sb = d.edge_sub_begin[3 * c + e];
             const std::uint32_t se = d.edge_sub_begin[3 * c + e + 1];
             g.sub_begin[e] = sb;
@@ -202,7 +203,7 @@ void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF6
                 if (d.sub_target[k] >= d.n_emitters) { throw std::invalid_argument("emitter index out of range"); }
                 link = -static_cast<int>(d.sub_target[k]) - 2;
             }
-            f.link[e] = link;
+            std::memcpy(&f.edge[e].w, &link, sizeof link);// the edge's link, as int bits
             f.rev |= (rev & 3U) << (2 * e);
             if (flip) { f.rev |= 1U << (8 + e); }
             for (std::uint32_t k = sb; k < se; ++k) {

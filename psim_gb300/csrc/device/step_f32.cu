@@ -175,8 +175,8 @@ template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, P
             r1 = 1.f - r1;
             r2 = 1.f - r2;
         }
-        p.px = c.vert[1].x * r1 + c.vert[2].x * r2;
-        p.py = c.vert[1].y * r1 + c.vert[2].y * r2;
+        p.px = c.v1.x * r1 + c.v2.x * r2;
+        p.py = c.v1.y * r1 + c.v2.y * r2;
         iso_dir(p, rs);
         return P.dt;
     }
@@ -262,6 +262,44 @@ template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P,
     L.v = vel32<S>(P, L.p.binw, meta_pol(L.p.meta), meta_phasor(L.p.meta));
 }
 
+// Earliest exit of the straight path p + w t from cell C through an edge other than 'entry':
+// the edge (or -1) and its time.
+__device__ __forceinline__ void next_exit(const CellF32* C, const Ph32& p, float wx, float wy, std::uint32_t entry, float& tbest,
+                                          int& ebest) {
+    tbest = 3.0e38f;
+    ebest = -1;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const float4 E = C->edge[e];
+        const float den = E.x * wx + E.y * wy;
+        if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
+            const float t = fmaxf(__fdividef(E.z - (E.x * p.px + E.y * p.py), den), 0.f);
+            if (t < tbest) {
+                tbest = t;
+                ebest = e;
+            }
+        }
+    }
+}
+
+// The phonon has reached its step's boundary: the outcome (alive into the next step or not,
+// tallied or not).  Returns true (the step is over).
+__device__ __forceinline__ bool boundary_outcome(const StepParams& P, const Lane& L, Outcome& out) {
+    const std::uint32_t next = L.step() + 1U;
+    out = Outcome{ false, true, false, false, 0U, 0, 0 };
+    if (next >= P.n_steps) { return true; }
+    out.alive = true;
+    out.cont = next < P.step + P.n_fused;
+    if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
+        const float sv = static_cast<float>(meta_sign(L.p.meta)) * L.v;
+        out.tallied = true;
+        out.sensor = L.sensor;
+        out.fx = __float2ll_rn(sv * L.p.dx * kFluxScale);
+        out.fy = __float2ll_rn(sv * L.p.dy * kFluxScale);
+    }
+    return true;
+}
+
 // One segment of a phonon's step: the straight flight to the next edge impact or to the end of
 // the current event (ModelSimulator::simulatePhonon / handleImpacts / nextImpact,
 // psim/src/modelSimulator.cpp:87-225).  Returns true when the phonon's step is over (it
@@ -295,21 +333,9 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
     const CellF32* C = cells_of<S>(P) + cell;
     const float wx = p.dx * L.v;
     const float wy = p.dy * L.v;
-    const std::uint32_t entry = meta_edge(p.meta);
-    float tbest = 3.0e38f;
-    int ebest = -1;
-#pragma unroll
-    for (int e = 0; e < 3; ++e) {
-        const float4 E = C->edge[e];
-        const float den = E.x * wx + E.y * wy;
-        if (static_cast<std::uint32_t>(e) != entry && den > 0.f) {
-            const float t = fmaxf(__fdividef(E.z - (E.x * p.px + E.y * p.py), den), 0.f);
-            if (t < tbest) {
-                tbest = t;
-                ebest = e;
-            }
-        }
-    }
+    float tbest;
+    int ebest;
+    next_exit(C, p, wx, wy, meta_edge(p.meta), tbest, ebest);
     const float left = L.target - L.drifted;
     bool event_over = true;
     if (ebest < 0 || tbest > left) {
@@ -321,7 +347,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
         p.py += wy * tbest;
         L.drifted += tbest;
         const float4 E = C->edge[ebest];
-        const int link = C->link[ebest];
+        const int link = edge_link(E);
         std::uint32_t entry_next = static_cast<std::uint32_t>(ebest);
         if (link >= 0) {// TransitionSurface::handlePhonon (psim/src/surface.cpp:71-109)
             const CellF32* N = cells_of<S>(P) + link;
@@ -364,8 +390,8 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
                 r1 = 1.f - r1;
                 r2 = 1.f - r2;
             }
-            p.px = C->vert[1].x * r1 + C->vert[2].x * r2;
-            p.py = C->vert[1].y * r1 + C->vert[2].y * r2;
+            p.px = C->v1.x * r1 + C->v2.x * r2;
+            p.py = C->v1.y * r1 + C->v2.y * r2;
             p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
             L.drifted = L.target;
             atomicAdd(P.counters + 1, 1ULL);
@@ -379,21 +405,7 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
     L.rem -= used;
     p.tts -= used;
     L.need_target = true;
-    if (L.rem == 0.f) {
-        const std::uint32_t next = L.step() + 1U;
-        out = Outcome{ false, true, false, false, 0U, 0, 0 };
-        if (next >= P.n_steps) { return true; }
-        out.alive = true;
-        out.cont = next < P.step + P.n_fused;
-        if (next >= P.step_adj && next - P.step_adj < P.n_recorded) {
-            const float sv = static_cast<float>(meta_sign(p.meta)) * L.v;
-            out.tallied = true;
-            out.sensor = L.sensor;
-            out.fx = __float2ll_rn(sv * p.dx * kFluxScale);
-            out.fy = __float2ll_rn(sv * p.dy * kFluxScale);
-        }
-        return true;
-    }
+    if (L.rem == 0.f) { return boundary_outcome(P, L, out); }
     if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
         if (!L.rates_ok) {// the scattering time was drawn in an earlier step: recompute its rates
             const float3 r = rates32(materials_of<S>(P)[L.mat], sensors_of<S>(P)[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
