@@ -240,7 +240,7 @@ struct alignas(8) TallySlot {
 };
 
 // Measurement steps one FP32 launch may cover (the shared-memory tally holds one slot per step).
-constexpr std::uint32_t kMaxFused = 8;
+constexpr std::uint32_t kMaxFused = 16;
 
 struct StepParams {
     // model

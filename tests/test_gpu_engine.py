@@ -57,11 +57,11 @@ def test_launch_shape_does_not_change_results(api, monkeypatch):
 
 @pytest.mark.parametrize("name", ["kinked_small", "plate_small", "bar_ss"])
 def test_steps_per_launch_do_not_change_results(api, monkeypatch, name):
-    """An FP32 launch covers up to 8 measurement steps and carries phonons across the inner
+    """An FP32 launch covers up to 16 measurement steps and carries phonons across the inner
     boundaries in registers.  Tallies, the population history and the phonon-step count equal
     those of one step per launch, with shared-memory tables and with global ones."""
     ref = None
-    for stage, fuse in (("1", "1"), ("1", "3"), ("1", "8"), ("0", "5")):
+    for stage, fuse in (("1", "1"), ("1", "3"), ("1", "8"), ("1", "16"), ("0", "5")):
         monkeypatch.setenv("PSIM_GB300_STAGE", stage)
         monkeypatch.setenv("PSIM_GB300_FUSE", fuse)
         m = api.Model(model_path(name))
@@ -88,7 +88,7 @@ def test_counters_and_phonon_steps(api):
     assert c["phonons"] > 90000
     assert c["phonon_steps"] > c["phonons"]
     # 1000 steps: ceil(1000 / steps per launch) transport launches and one population pass
-    assert 1 <= c["steps_per_launch"] <= 8
+    assert 1 <= c["steps_per_launch"] <= 16
     assert c["transport_launches"] == -(-1000 // c["steps_per_launch"])
     assert c["kernel_launches"] == c["transport_launches"] + 1
     assert c["max_population"] > 0
