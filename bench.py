@@ -185,6 +185,7 @@ def main():
     ap.add_argument("--population-out", default="", help="write the phonon population per step of the last timed run (JSON)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP32-vs-FP64 same-stream comparison")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -299,6 +300,25 @@ def main():
         e2e = {"value": e_total / e_wall, "unit": "phonon-steps/s", "h2d_bytes_per_step": int(h2d / args.steps),
                "d2h_bytes_per_step": int(d2h / args.steps)}
 
+    # FP32 error against the FP64 kernel on the same random streams: the same geometry at a
+    # budget the FP64 kernel runs in seconds (outside the timed region)
+    fp64_check = None
+    if rank == 0 and world == 1 and not args.no_fp64_check and precision == api.FP32:
+        per_step = 2.0e4
+        small = api.Model(model_json(os.path.join(td, "kinked_fp64.json"), int(per_step * steps_n / lifetime), steps_n,
+                                     args.dt_ps))
+        t32, t64 = [], []
+        for seed in range(1, 5):
+            t32.append(small.run(seed=seed, precision=api.FP32).measurements()[:, 0])
+            t64.append(small.run(seed=seed, precision=api.FP64).measurements()[:, 0])
+        t32, t64 = np.array(t32), np.array(t64)
+        diff = np.abs(t32 - t64)
+        noise = t64.std(axis=0, ddof=1).mean()
+        fp64_check = {"workload": f"the same model at {per_step:.0e} phonons per step, 4 seeds, FP32 and FP64 kernels on the same random streams",
+                      "quantity": "per-sensor mean temperature over the run",
+                      "mean_abs_diff_K": float(diff.mean()), "max_abs_diff_K": float(diff.max()),
+                      "seed_to_seed_sd_K": float(noise), "mean_diff_over_sd": float(diff.mean() / noise)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -321,7 +341,7 @@ def main():
                        "precision": args.precision, "bench_step": "one full simulation run",
                        "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
-            "clocks": clk, "wall_s_timed": wall, "steady_state": steady,
+            "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

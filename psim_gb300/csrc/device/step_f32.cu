@@ -414,14 +414,13 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
             L.fNU = (r.x + r.y) * inv;
         }
         const float u = rs.uf();
-        if (u <= L.fNU) {// normal or Umklapp: resample frequency, velocity and polarization
+        const bool resample = u <= L.fNU;                          // normal or Umklapp
+        const bool redirect = resample ? (u > L.fN) : (L.fNU < 1.f);// Umklapp, or impurity (positive rate)
+        if (resample) {// new frequency, velocity and polarization
             sample_freq<S>(P, p, rs, sensors_of<S>(P)[L.sensor].scatter_table, L.mat);
             L.v = vel32<S>(P, p.binw, meta_pol(p.meta), phasor);
-            if (u > L.fN) {// Umklapp: also a new direction
-                iso_dir(p, rs);
-                p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
-            }
-        } else if (L.fNU < 1.f) {// impurity (its rate is positive): new direction only
+        }
+        if (redirect) {// new direction
             iso_dir(p, rs);
             p.meta = meta_with_cell_edge(p.meta, cell, kNoEdge);
         }
