@@ -356,6 +356,9 @@ psim::gpu::InterpDesc interp_from(const psim_interp_desc* d) {
     const std::size_t nt = o.mat_temp_begin.empty() ? 0 : static_cast<std::size_t>(o.mat_temp_begin.back());
     o.temps = copy_of(d->temps, nt, "temps");
     o.energies = copy_of(d->energies, nt, "energies");
+    for (std::size_t m = 0; m + 1 < o.mat_temp_begin.size(); ++m) {
+        if (o.mat_temp_begin[m + 1] < o.mat_temp_begin[m]) { throw std::invalid_argument("mat_temp_begin decreases"); }
+    }
     for (auto m : o.material) {
         if (m >= d->n_materials) { throw std::invalid_argument("sensor material out of range"); }
         if (o.mat_temp_begin[m + 1] <= o.mat_temp_begin[m]) { throw std::invalid_argument("material has an empty temperature grid"); }

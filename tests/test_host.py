@@ -207,6 +207,23 @@ def test_gpu_entry_points_fail_loudly_without_a_device(api):
         api.geom_intersect(g["intersect_a"][:4], g["intersect_b"][:4])
 
 
+def test_interpreter_rejects_decreasing_material_offsets(api):
+    """A second material whose temperature-grid offset decreases would let the first material's
+    lookups run past the grid the call copies: refused before any device work."""
+    import ctypes
+    m = api.Model(model_path("bar_ss"))
+    d = m.interp_desc()
+    assert d.n_materials == 1
+    n = int(np.ctypeslib.as_array(d.mat_temp_begin, shape=(2,))[1])
+    bad = np.array([0, n, n // 2], dtype=np.uint64)
+    d.n_materials = 2
+    d.mat_temp_begin = bad.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    counts = np.zeros((d.n_sensors, d.recorded_steps), dtype=np.int64)
+    with pytest.raises(api.PsimError) as e:
+        api.final_temps(d, counts, 0)
+    assert e.value.code == api.PSIM_ERR_INVALID and "decreases" in str(e.value)
+
+
 def test_modelgen_workloads_load(api):
     from psim_gb300 import modelgen as mg
     with tempfile.TemporaryDirectory() as td:
