@@ -186,6 +186,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP32-vs-FP64 same-stream comparison")
+    ap.add_argument("--batch-models", type=int, default=64,
+                    help="models of the batched workload (random rectangles) to time concurrently; 0 skips it")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -319,6 +321,29 @@ def main():
                       "mean_abs_diff_K": float(diff.mean()), "max_abs_diff_K": float(diff.max()),
                       "seed_to_seed_sd_K": float(noise), "mean_diff_over_sd": float(diff.mean() / noise)}
 
+    # the batched workload: independent random rectangles (uneven cells and populations) run
+    # concurrently, options from the autotuner, against the same models one at a time
+    batch = None
+    if rank == 0 and world == 1 and args.batch_models > 0:
+        from psim_gb300 import modelgen as mg
+        paths = [mg.write(mg.random_bar(1000 + i), os.path.join(td, f"rect_{i}.json")) for i in range(args.batch_models)]
+        models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in enumerate(paths)]
+        opt, tuned_rate = api.batch_autotune(models, sample=min(16, len(models)))
+        secs, steps_b = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
+        t0 = time.perf_counter()
+        steps_s = 0
+        for i, m in enumerate(models):
+            m.run(seed=i + 1, precision=precision)
+            steps_s += m.counters()["phonon_steps"]
+        secs_s = time.perf_counter() - t0
+        batch = {"workload": f"{len(models)} random rectangles: length U(0.2, 5) um, width U(50, 500) nm, 4-200 cells, "
+                             "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
+                             "3000 steps of 5 ps, steady state",
+                 "autotuned": {"workers": opt.workers, "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate,
+                               "pilot_models": min(16, len(models))},
+                 "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
+                 "one_at_a_time": {"value": steps_s / secs_s, "seconds": secs_s}}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -341,7 +366,7 @@ def main():
                        "precision": args.precision, "bench_step": "one full simulation run",
                        "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
-            "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check,
+            "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check, "batch": batch,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

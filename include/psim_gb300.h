@@ -109,6 +109,28 @@ int psim_model_export(const psim_model* m, const char* json_path, double seconds
 void psim_model_destroy(psim_model* m);
 
 /* ------------------------------------------------------------------------------------------
+ * Many independent models on one GPU.  No counterpart in the reference, which runs one model
+ * per process (psim/src/main.cpp:10-31 loops over its input files).  A host work queue hands
+ * the models to `workers` threads, each with its own CUDA stream; each model runs as
+ * psim_model_run would (its own seed, precision and steady-state stop), its transport launches
+ * limited to `max_blocks` thread blocks so that small models share the GPU.  A model's results
+ * do not depend on the batch it ran in.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct psim_batch_options {
+    int32_t workers;    /* host threads, one CUDA stream each (>= 1) */
+    int32_t max_blocks; /* thread blocks per transport launch (0: one per multiprocessor) */
+} psim_batch_options;
+/* Runs every model once; fails with the first model's failure after the others stopped.
+ * seconds (may be NULL): wall time; phonon_steps (may be NULL): over all models. */
+int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_options* opt, double* seconds,
+                   uint64_t* phonon_steps);
+/* The autotuner: runs the first `sample` models under each candidate (workers 4, 8, 16 x blocks
+ * per launch 1/8, 1/4, 1/2 and all of the multiprocessors) and returns the fastest options and
+ * their rate (phonon-steps/s; may be NULL). */
+int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, psim_batch_options* out,
+                        double* best_rate);
+
+/* ------------------------------------------------------------------------------------------
  * Simulator seam: ModelSimulator (psim/include/psim/modelSimulator.h:12-41).
  * The caller keeps ownership of every array in the description; psim_sim_create copies it.
  * Indices are 0-based positions in the caller's arrays.

@@ -80,6 +80,10 @@ class InterpDesc(ctypes.Structure):
     ]
 
 
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_int32), ("max_blocks", ctypes.c_int32)]
+
+
 # Every symbol the C header declares, with (restype, argtypes).
 SIGNATURES = {
     "psim_last_error": (ctypes.c_char_p, []),
@@ -125,6 +129,10 @@ SIGNATURES = {
                                                 ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64]),
     "psim_model_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
     "psim_sim_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
+    "psim_batch_run": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.POINTER(BatchOptions),
+                                      _c_dp, _c_u64p]),
+    "psim_batch_autotune": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.POINTER(BatchOptions), _c_dp]),
     "psim_geom_intersect": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
@@ -207,6 +215,11 @@ class Model:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_options(self, seed: int = 1, precision: int = FP32, stream: Optional[int] = None) -> "Model":
+        """Seed, precision and stream of later runs (psim_model_set_options)."""
+        _check(lib().psim_model_set_options(self._h, seed, precision, ctypes.c_void_p(stream or 0)))
+        return self
 
     def run(self, seed: int = 1, precision: int = FP32, stream: Optional[int] = None) -> "Model":
         _check(lib().psim_model_set_options(self._h, seed, precision, ctypes.c_void_p(stream or 0)))
@@ -354,6 +367,35 @@ def interpret(desc: InterpDesc, energy: np.ndarray, flux: np.ndarray):
     stats = np.zeros((S, 6))
     _check(lib().psim_interpret(ctypes.byref(desc), _i64(energy), _dp(flux), _dp(temps), _dp(fluxes), _dp(stats)))
     return temps, fluxes, stats
+
+
+def _handles(models):
+    arr = (ctypes.c_void_p * max(1, len(models)))()
+    for i, m in enumerate(models):
+        arr[i] = m._h
+    return arr
+
+
+def batch_run(models, workers: int = 8, max_blocks: int = 0) -> Tuple[float, int]:
+    """Runs every Model once, concurrently (psim_batch_run): (wall seconds, phonon-steps)."""
+    opt = BatchOptions(workers, max_blocks)
+    secs = ctypes.c_double()
+    steps = ctypes.c_uint64()
+    _check(lib().psim_batch_run(_handles(models), len(models), ctypes.byref(opt), ctypes.byref(secs),
+                                ctypes.byref(steps)))
+    for m in models:
+        m._shape()
+    return float(secs.value), int(steps.value)
+
+
+def batch_autotune(models, sample: int = 16) -> Tuple[BatchOptions, float]:
+    """The batch autotuner (psim_batch_autotune): the fastest options and their phonon-steps/s."""
+    opt = BatchOptions()
+    rate = ctypes.c_double()
+    _check(lib().psim_batch_autotune(_handles(models), len(models), sample, ctypes.byref(opt), ctypes.byref(rate)))
+    for m in models[:sample]:
+        m._shape()
+    return opt, float(rate.value)
 
 
 def _steady(fn, handle, n_sensors: int, window: int, batches: int, z: float, patience: int) -> Tuple[int, np.ndarray]:

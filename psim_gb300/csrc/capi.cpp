@@ -10,6 +10,7 @@
 #include <string>
 
 #include "device/engine.hpp"
+#include "host/batch.hpp"
 #include "host/model.hpp"
 
 struct psim_model {
@@ -450,6 +451,40 @@ int psim_sim_steps_run(const psim_sim* s, uint64_t* steps) {
     if (s == nullptr || steps == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     *steps = s->e->steps_run();
     return PSIM_OK;
+}
+
+// ------------------------------------------------------------------ batches of models
+namespace {
+std::vector<psim::HostModel*> batch_models(psim_model* const* models, int32_t n) {
+    if (n < 0 || (n > 0 && models == nullptr)) { throw std::invalid_argument("bad model list"); }
+    std::vector<psim::HostModel*> v;
+    for (int32_t i = 0; i < n; ++i) {
+        if (models[i] == nullptr) { throw std::invalid_argument("null model in the batch"); }
+        v.push_back(models[i]->m.get());
+    }
+    return v;
+}
+}// namespace
+
+int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_options* opt, double* seconds, uint64_t* phonon_steps) {
+    if (opt == nullptr) { return fail(PSIM_ERR_INVALID, "null options"); }
+    return guard([&]() {
+        psim::BatchOptions o;
+        o.workers = opt->workers;
+        o.max_blocks = opt->max_blocks;
+        const psim::BatchResult r = psim::run_batch(batch_models(models, n), o);
+        if (seconds != nullptr) { *seconds = r.seconds; }
+        if (phonon_steps != nullptr) { *phonon_steps = r.phonon_steps; }
+    });
+}
+
+int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, psim_batch_options* out, double* best_rate) {
+    if (out == nullptr) { return fail(PSIM_ERR_INVALID, "null options"); }
+    return guard([&]() {
+        const psim::BatchOptions o = psim::autotune_batch(batch_models(models, n), sample, best_rate);
+        out->workers = o.workers;
+        out->max_blocks = o.max_blocks;
+    });
 }
 
 int psim_final_temps_noalloc(const psim_interp_desc* d, const int64_t* energy_dev, uint64_t start_step, double* out_dev,

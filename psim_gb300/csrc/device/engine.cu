@@ -26,8 +26,9 @@ void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream
 int occupancy_f32(bool staged, int block, std::size_t smem);
 int occupancy_f64(std::size_t smem);
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
-                      double* stats_h, cudaStream_t stream);
-void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream);
+                      double* stats_h, cudaStream_t stream, InterpCache* cache);
+void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream,
+                        InterpCache* cache);
 
 namespace {
 
@@ -222,6 +223,7 @@ void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF6
 
 struct Engine::Impl {
     Buf cells32, cells64, subs64, sensors, materials, emitters, alias, centre32, vel32, centre64, vel64;
+    InterpCache* interp{ nullptr };// the interpreter's buffers, reused by every read-out
     std::vector<EmitterDev> emit_host;
     std::vector<BirthGroup> groups;
     std::vector<std::uint32_t> group_begin;// [N+1]
@@ -241,7 +243,35 @@ struct Engine::Impl {
     cudaEvent_t ev0{ nullptr }, ev1{ nullptr };
     cudaStream_t own{ nullptr };
     int sms{ 0 };
+
+    Impl() = default;
+    Impl(const Impl&) = delete;
+    Impl& operator=(const Impl&) = delete;
+    ~Impl() {// also when the engine's constructor throws part-way
+        if (ev0 != nullptr) { cudaEventDestroy(ev0); }
+        if (ev1 != nullptr) { cudaEventDestroy(ev1); }
+        if (own != nullptr) { cudaStreamDestroy(own); }
+        interp_cache_destroy(interp);
+    }
 };
+
+void* create_stream() {
+    cudaStream_t s = nullptr;
+    check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+    return s;
+}
+
+void destroy_stream(void* stream) noexcept {
+    if (stream != nullptr) { cudaStreamDestroy(static_cast<cudaStream_t>(stream)); }
+}
+
+int sm_count() {
+    int dev = 0;
+    int sms = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    return sms;
+}
 
 int device_count() noexcept {
     int n = 0;
@@ -265,6 +295,7 @@ Engine::Engine(const SimDesc& d)
     check(cudaGetDevice(&dev), "cudaGetDevice");
     check(cudaDeviceGetAttribute(&I.sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
     check(cudaStreamCreateWithFlags(&I.own, cudaStreamNonBlocking), "stream");
+    I.interp = interp_cache_create();
     stream_ = I.own;
     check(cudaEventCreate(&I.ev0), "event");
     check(cudaEventCreate(&I.ev1), "event");
@@ -397,13 +428,7 @@ Engine::Engine(const SimDesc& d)
     check(cudaMemset(I.tally.p, 0, I.tally.bytes), "memset tally");
 }
 
-Engine::~Engine() {
-    if (impl_) {
-        if (impl_->ev0 != nullptr) { cudaEventDestroy(impl_->ev0); }
-        if (impl_->ev1 != nullptr) { cudaEventDestroy(impl_->ev1); }
-        if (impl_->own != nullptr) { cudaStreamDestroy(impl_->own); }
-    }
-}
+Engine::~Engine() = default;
 
 std::uint64_t Engine::init_builders(double t_eq, double eff_energy, const double* cell_energy, const double* emit_energy,
                                     const double* sensor_init_temp, std::uint64_t seed) {
@@ -795,7 +820,8 @@ void Engine::tallies(std::int64_t* energy, double* flux, std::uint64_t K) const 
 void Engine::interpret(const InterpDesc& d, double* temps, double* fluxes, double* stats) const {
     Impl& I = *impl_;
     unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p, d.recorded);
-    interpret_device(d, I.unpacked_energy.as<long long>(), I.unpacked_flux.as<double>(), temps, fluxes, stats, I.own);
+    interpret_device(d, I.unpacked_energy.as<long long>(), I.unpacked_flux.as<double>(), temps, fluxes, stats, I.own,
+                     I.interp);
     const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
     counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
                            + d.material.size() * 4 + d.mat_temp_begin.size() * 8;
@@ -813,7 +839,7 @@ long long Engine::steady_onset(const SteadyCriterion& c, long long* per_sensor) 
 void Engine::final_temps(const InterpDesc& d, std::uint64_t start, double* out) const {
     Impl& I = *impl_;
     unpack(*this, I.unpacked_energy, I.unpacked_flux, I.own, I.tally.p, d.recorded);
-    final_temps_device(d, I.unpacked_energy.as<long long>(), start, out, I.own);
+    final_temps_device(d, I.unpacked_energy.as<long long>(), start, out, I.own, I.interp);
     counters_.h2d_bytes += (d.area.size() + d.heat_capacity.size() + d.init_temp.size() + d.temps.size() + d.energies.size()) * sizeof(double)
                            + d.material.size() * 4 + d.mat_temp_begin.size() * 8;
     counters_.d2h_bytes += d.n_sensors * 8ULL;

@@ -152,6 +152,11 @@ long long steady_onset_device(const void* tally, std::uint32_t S, std::uint64_t 
 long long steady_onset_host(const std::int64_t* energy, const double* flux, std::uint32_t S, std::uint64_t K,
                             const SteadyCriterion& c, long long* per_sensor);
 
+// Device buffers an engine keeps for its interpretations (device/interpret.cu).
+struct InterpCache;
+InterpCache* interp_cache_create();
+void interp_cache_destroy(InterpCache* c) noexcept;
+
 // Stand-alone interpreter on host arrays (psim_interpret / psim_final_temps).
 void interpret_host(const InterpDesc& d, const std::int64_t* energy, const double* flux, double* temps, double* fluxes,
                     double* stats);
@@ -188,5 +193,10 @@ void geom_tri_contains(std::int64_t n, const double* tris, const double* pts, st
 void geom_edge_index(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
 
 int device_count() noexcept;
+// A non-blocking CUDA stream of the current device (as void*), and its release.
+void* create_stream();
+void destroy_stream(void* stream) noexcept;
+// Multiprocessors of the current device.
+int sm_count();
 
 }// namespace psim::gpu

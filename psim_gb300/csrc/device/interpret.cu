@@ -151,45 +151,60 @@ __global__ void scale_kernel(InterpDev d, double* temps, const double* flux, dou
     mean_se(K, [&](std::uint64_t i) { return out[2 * i + 1]; }, st + 4, st + 5);
 }
 
-// ---------------------------------------------------------------- device buffers for one interpretation
+// ---------------------------------------------------------------- device buffers for interpretations
+// A buffer that only grows: reused across calls, so an engine's repeated interpretations do not
+// allocate (a cudaFree would wait for every stream of the device, runs of other models too).
 struct DevBuf {
     void* p{ nullptr };
+    std::size_t cap{ 0 };
     DevBuf() = default;
-    explicit DevBuf(std::size_t bytes) { check(cudaMalloc(&p, bytes > 0 ? bytes : 16), "cudaMalloc"); }
+    explicit DevBuf(std::size_t bytes) { reserve(bytes); }
     ~DevBuf() {
         if (p != nullptr) { cudaFree(p); }
     }
     DevBuf(const DevBuf&) = delete;
     DevBuf& operator=(const DevBuf&) = delete;
+    void reserve(std::size_t bytes) {
+        bytes = std::max<std::size_t>(bytes, 16);
+        if (bytes <= cap) { return; }
+        if (p != nullptr) { cudaFree(p); }
+        p = nullptr;
+        cap = 0;
+        check(cudaMalloc(&p, bytes), "cudaMalloc");
+        cap = bytes;
+    }
     template<typename T> T* as() const { return static_cast<T*>(p); }
 };
 
-template<typename T> void upload(DevBuf& b, const std::vector<T>& v) {
-    if (!v.empty()) { check(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload"); }
+template<typename T> void upload(DevBuf& b, const std::vector<T>& v, cudaStream_t stream) {
+    b.reserve(v.size() * sizeof(T));
+    if (!v.empty()) { check(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream), "upload"); }
 }
 
-struct InterpOnDevice {
-    DevBuf area, heat, init, mat, mtb, temps, energies;
-    InterpDev dev{};
-    explicit InterpOnDevice(const InterpDesc& d)
-        : area(d.area.size() * sizeof(double))
-        , heat(d.heat_capacity.size() * sizeof(double))
-        , init(d.init_temp.size() * sizeof(double))
-        , mat(d.material.size() * sizeof(std::uint32_t))
-        , mtb(d.mat_temp_begin.size() * sizeof(std::uint64_t))
-        , temps(d.temps.size() * sizeof(double))
-        , energies(d.energies.size() * sizeof(double)) {
-        upload(area, d.area);
-        upload(heat, d.heat_capacity);
-        upload(init, d.init_temp);
-        upload(mat, d.material);
-        upload(mtb, d.mat_temp_begin);
-        upload(temps, d.temps);
-        upload(energies, d.energies);
-        dev = InterpDev{ d.n_sensors, d.recorded, d.t_eq, d.eff_energy, d.lb, d.ub, area.as<double>(), heat.as<double>(),
-            init.as<double>(), mat.as<std::uint32_t>(), mtb.as<std::uint64_t>(), temps.as<double>(), energies.as<double>() };
-    }
+}// namespace
+
+// The interpreter's device buffers of one engine (or of one stand-alone call).
+struct InterpCache {
+    DevBuf area, heat, init, mat, mtb, temps, energies;// the description's tables
+    DevBuf out_temps, out_fluxes, out_stats, out_final;
 };
+
+InterpCache* interp_cache_create() { return new InterpCache(); }
+void interp_cache_destroy(InterpCache* c) noexcept { delete c; }
+
+namespace {
+
+InterpDev upload_interp(const InterpDesc& d, InterpCache& c, cudaStream_t stream) {
+    upload(c.area, d.area, stream);
+    upload(c.heat, d.heat_capacity, stream);
+    upload(c.init, d.init_temp, stream);
+    upload(c.mat, d.material, stream);
+    upload(c.mtb, d.mat_temp_begin, stream);
+    upload(c.temps, d.temps, stream);
+    upload(c.energies, d.energies, stream);
+    return InterpDev{ d.n_sensors, d.recorded, d.t_eq, d.eff_energy, d.lb, d.ub, c.area.as<double>(), c.heat.as<double>(),
+        c.init.as<double>(), c.mat.as<std::uint32_t>(), c.mtb.as<std::uint64_t>(), c.temps.as<double>(), c.energies.as<double>() };
+}
 
 int blocks_for(std::uint64_t n, int block) { return static_cast<int>(std::min<std::uint64_t>((n + block - 1) / block, 65535ULL * 16ULL)); }
 
@@ -197,14 +212,19 @@ int blocks_for(std::uint64_t n, int block) { return static_cast<int>(std::min<st
 
 // Interpretation with the tallies already on the device (energy [S][K], flux [S][K][2]).
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
-                      double* stats_h, cudaStream_t stream) {
-    InterpOnDevice id(d);
+                      double* stats_h, cudaStream_t stream, InterpCache* cache) {
+    InterpCache local;
+    InterpCache& c = cache != nullptr ? *cache : local;
+    const InterpDev dev = upload_interp(d, c, stream);
     const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
-    DevBuf temps(SK * sizeof(double));
-    DevBuf fluxes(SK * 2 * sizeof(double));
-    DevBuf stats(static_cast<std::size_t>(d.n_sensors) * 6 * sizeof(double));
-    if (SK > 0) { temps_kernel<<<std::max(1, blocks_for(SK, 256)), 256, 0, stream>>>(id.dev, energy, 0, temps.as<double>()); }
-    scale_kernel<<<std::max(1U, (d.n_sensors + 127) / 128), 128, 0, stream>>>(id.dev, temps.as<double>(), flux,
+    DevBuf& temps = c.out_temps;
+    DevBuf& fluxes = c.out_fluxes;
+    DevBuf& stats = c.out_stats;
+    temps.reserve(SK * sizeof(double));
+    fluxes.reserve(SK * 2 * sizeof(double));
+    stats.reserve(static_cast<std::size_t>(d.n_sensors) * 6 * sizeof(double));
+    if (SK > 0) { temps_kernel<<<std::max(1, blocks_for(SK, 256)), 256, 0, stream>>>(dev, energy, 0, temps.as<double>()); }
+    scale_kernel<<<std::max(1U, (d.n_sensors + 127) / 128), 128, 0, stream>>>(dev, temps.as<double>(), flux,
                                                                                fluxes.as<double>(), stats.as<double>());
     check(cudaGetLastError(), "interpret kernels");
     if (temps_h != nullptr) { check(cudaMemcpyAsync(temps_h, temps.p, SK * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy temps"); }
@@ -213,14 +233,19 @@ void interpret_device(const InterpDesc& d, const long long* energy, const double
     check(cudaStreamSynchronize(stream), "interpret sync");
 }
 
-void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream) {
+void final_temps_device(const InterpDesc& d, const long long* energy, std::uint64_t start, double* out_h, cudaStream_t stream,
+                        InterpCache* cache) {
     if (start > d.recorded) { throw std::invalid_argument("start step beyond the recorded steps"); }
-    InterpOnDevice id(d);
+    InterpCache local;
+    InterpCache& c = cache != nullptr ? *cache : local;
+    const InterpDev dev = upload_interp(d, c, stream);
     const std::uint64_t n = static_cast<std::uint64_t>(d.n_sensors) * (d.recorded - start);
-    DevBuf temps(n * sizeof(double));
-    DevBuf out(static_cast<std::size_t>(d.n_sensors) * sizeof(double));
-    if (n > 0) { temps_kernel<<<std::max(1, blocks_for(n, 256)), 256, 0, stream>>>(id.dev, energy, start, temps.as<double>()); }
-    final_kernel<<<std::max(1U, (d.n_sensors + 127) / 128), 128, 0, stream>>>(id.dev, temps.as<double>(), start, out.as<double>());
+    DevBuf& temps = c.out_temps;
+    DevBuf& out = c.out_final;
+    temps.reserve(n * sizeof(double));
+    out.reserve(static_cast<std::size_t>(d.n_sensors) * sizeof(double));
+    if (n > 0) { temps_kernel<<<std::max(1, blocks_for(n, 256)), 256, 0, stream>>>(dev, energy, start, temps.as<double>()); }
+    final_kernel<<<std::max(1U, (d.n_sensors + 127) / 128), 128, 0, stream>>>(dev, temps.as<double>(), start, out.as<double>());
     check(cudaGetLastError(), "final temps kernels");
     check(cudaMemcpyAsync(out_h, out.p, d.n_sensors * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy final temps");
     check(cudaStreamSynchronize(stream), "final temps sync");
@@ -233,14 +258,14 @@ void interpret_host(const InterpDesc& d, const std::int64_t* energy, const doubl
     DevBuf f(SK * 2 * sizeof(double));
     check(cudaMemcpy(e.p, energy, SK * sizeof(long long), cudaMemcpyHostToDevice), "upload energy");
     check(cudaMemcpy(f.p, flux, SK * 2 * sizeof(double), cudaMemcpyHostToDevice), "upload flux");
-    interpret_device(d, e.as<long long>(), f.as<double>(), temps, fluxes, stats, nullptr);
+    interpret_device(d, e.as<long long>(), f.as<double>(), temps, fluxes, stats, nullptr, nullptr);
 }
 
 void final_temps_host(const InterpDesc& d, const std::int64_t* energy, std::uint64_t start, double* out) {
     const std::uint64_t SK = static_cast<std::uint64_t>(d.n_sensors) * d.recorded;
     DevBuf e(SK * sizeof(long long));
     check(cudaMemcpy(e.p, energy, SK * sizeof(long long), cudaMemcpyHostToDevice), "upload energy");
-    final_temps_device(d, e.as<long long>(), start, out, nullptr);
+    final_temps_device(d, e.as<long long>(), start, out, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------- final temperatures without allocation

@@ -556,13 +556,25 @@ void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem,
     }
 }
 
+// Blocks per multiprocessor for this launch shape, 0 when it cannot launch.  The kernel's
+// dynamic shared-memory limit is a process-wide attribute: it is always raised to the device's
+// maximum (the same value for every caller), never to one model's need, so engines that run
+// side by side on other threads cannot lower it under each other's launches.
 int occupancy_f32(bool staged, int block, std::size_t smem) {
     const void* fn = staged ? reinterpret_cast<const void*>(step_kernel_f32<true>) : reinterpret_cast<const void*>(step_kernel_f32<false>);
-    if (smem > 48 * 1024) {
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
+    int dev = 0;
+    int optin = 0;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess
+        || cudaFuncGetAttributes(&fa, fn) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int max_dynamic = optin - static_cast<int>(fa.sharedSizeBytes);
+    if (static_cast<long long>(smem) > max_dynamic) { return 0; }
+    if (max_dynamic > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dynamic) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
     }
     int blocks = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, block, smem) != cudaSuccess) {

@@ -517,6 +517,7 @@ void HostModel::run() {
         const std::uint64_t run_seed = seed_ * 0x9E3779B97F4A7C15ULL + run * 0xD1B54A32D192ED03ULL + 1;
         engine_->init_builders(t_eq_, eff_energy_, cell_energy.data(), emit_energy.data(), sensor_t0.data(), run_seed);
         engine_->set_steady_stop(stop_on_, stop_crit_, stop_check_);
+        engine_->set_grid(grid_);
         engine_->run(precision_, stream_);
         recorded_ = std::min<std::size_t>(desc_.recorded, engine_->steps_run());
         if (type_ == SimType::SteadyState) {

@@ -78,6 +78,11 @@ public:
         precision_ = precision;
         stream_ = stream;
     }
+    void set_stream(void* stream) noexcept { stream_ = stream; }
+    void* stream() const noexcept { return stream_; }
+    // Thread blocks per transport launch (0: one per multiprocessor, the default).
+    void set_grid(int blocks) noexcept { grid_ = blocks; }
+    int grid() const noexcept { return grid_; }
     // Stop each run once its recorded steps are steady (single-run periodic or transient models).
     void set_steady_stop(bool on, const gpu::SteadyCriterion& c, std::uint64_t check_every) {
         if (on) { gpu::validate_steady(c); }
@@ -135,6 +140,7 @@ private:
     std::uint64_t seed_{ 1 };
     int precision_{ 0 };
     void* stream_{ nullptr };
+    int grid_{ 0 };
     bool stop_on_{ false };
     gpu::SteadyCriterion stop_crit_{};
     std::uint64_t stop_check_{ 0 };
