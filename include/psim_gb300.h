@@ -124,7 +124,7 @@ typedef struct psim_batch_options {
  * seconds (may be NULL): wall time; phonon_steps (may be NULL): over all models. */
 int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_options* opt, double* seconds,
                    uint64_t* phonon_steps);
-/* The autotuner: runs the first `sample` models under each candidate (workers 4, 8, 16 x blocks
+/* The autotuner: runs the first `sample` models under each candidate (workers 4, 8, 16, 32 x blocks
  * per launch 1/8, 1/4, 1/2 and all of the multiprocessors) and returns the fastest options and
  * their rate (phonon-steps/s; may be NULL). */
 int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, psim_batch_options* out,
