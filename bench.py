@@ -328,7 +328,7 @@ def main():
         from psim_gb300 import modelgen as mg
         paths = [mg.write(mg.random_bar(1000 + i), os.path.join(td, f"rect_{i}.json")) for i in range(args.batch_models)]
         models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in enumerate(paths)]
-        opt, tuned_rate = api.batch_autotune(models, sample=min(16, len(models)))
+        opt, tuned_rate = api.batch_autotune(models, sample=min(8, len(models)))
         secs, steps_b = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
         t0 = time.perf_counter()
         steps_s = 0
@@ -340,7 +340,7 @@ def main():
                              "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
                              "3000 steps of 5 ps, steady state",
                  "autotuned": {"workers": opt.workers, "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate,
-                               "pilot_models": min(16, len(models))},
+                               "pilot_models": min(8, len(models))},
                  "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
                  "one_at_a_time": {"value": steps_s / secs_s, "seconds": secs_s}}
 
