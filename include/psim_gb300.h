@@ -103,10 +103,39 @@ int psim_model_sim_desc(const psim_model* m, struct psim_sim_desc* out);
  * with the given energy per phonon (<= 0: the model's initial total energy / num_phonons).
  * Arrays point into the model (valid until the next call on it).  Host only. */
 int psim_model_interp_desc(const psim_model* m, double eff_energy, struct psim_interp_desc* out);
+/* Warm start (no counterpart in the reference, whose runs start from the JSON's "t_init"): the
+ * temperature each sensor starts later runs from, in file order (temps[S]; NULL restores the
+ * file's).  It sets the cells' initial phonon energy and the first recorded temperature; the
+ * material tables and heat capacities stay at the file's t_init, so a warm run solves the same
+ * linearised problem as a cold one and reaches the same steady state.  Deviational models only
+ * (t_eq > 0); each temperature positive and finite.  psim_model_start_temps: out[S]. */
+int psim_model_start_temps(const psim_model* m, double* out);
+int psim_model_set_start_temps(psim_model* m, const double* temps);
 /* OutputManager::exportResults (psim/src/outputManager.cpp:13-38): writes ss_<name>.txt or
  * per_<name>.txt next to json_path with the given time in the header. */
 int psim_model_export(const psim_model* m, const char* json_path, double seconds);
 void psim_model_destroy(psim_model* m);
+
+/* ------------------------------------------------------------------------------------------
+ * The warm-start surrogate: a multilayer perceptron on the GPU (no counterpart in the
+ * reference).  widths[0] inputs, widths[1..n-2] GELU hidden layers, widths[n-1] linear outputs;
+ * BF16 parameters and activations, FP32 accumulation, mean-squared-error loss, Adam (beta 0.9 /
+ * 0.999) on FP32 master weights.  Parameters are laid out per layer as W[in][out] then b[out].
+ * Rows are float32 x[n][in], y[n][out].
+ * ------------------------------------------------------------------------------------------ */
+typedef struct psim_mlp psim_mlp;
+int psim_mlp_create(const int32_t* widths, int32_t n_widths, uint64_t seed, psim_mlp** out);
+int psim_mlp_n_params(const psim_mlp* net, uint64_t* n);
+int psim_mlp_get_params(const psim_mlp* net, float* out);
+int psim_mlp_set_params(psim_mlp* net, const float* in);
+/* Loss over the n rows and its gradient for every parameter (grads may be NULL). */
+int psim_mlp_gradients(psim_mlp* net, const float* x, const float* y, int32_t n, float* loss, float* grads);
+/* Adam over shuffled whole batches for `epochs` passes; final_loss (may be NULL): the last
+ * epoch's mean batch loss. */
+int psim_mlp_train(psim_mlp* net, const float* x, const float* y, int32_t n, int32_t batch, int32_t epochs, float lr,
+                   uint64_t seed, float* final_loss);
+int psim_mlp_predict(psim_mlp* net, const float* x, int32_t n, float* y);
+void psim_mlp_destroy(psim_mlp* net);
 
 /* ------------------------------------------------------------------------------------------
  * Many independent models on one GPU.  No counterpart in the reference, which runs one model

@@ -34,6 +34,7 @@ _c_u32p = ctypes.POINTER(ctypes.c_uint32)
 _c_i32p = ctypes.POINTER(ctypes.c_int32)
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _c_u64p = ctypes.POINTER(ctypes.c_uint64)
+_c_fp = ctypes.POINTER(ctypes.c_float)
 
 
 class PsimError(RuntimeError):
@@ -133,6 +134,17 @@ SIGNATURES = {
                                       _c_dp, _c_u64p]),
     "psim_batch_autotune": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int32,
                                            ctypes.POINTER(BatchOptions), _c_dp]),
+    "psim_model_start_temps": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "psim_model_set_start_temps": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "psim_mlp_create": (ctypes.c_int, [_c_i32p, ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    "psim_mlp_n_params": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
+    "psim_mlp_get_params": (ctypes.c_int, [ctypes.c_void_p, _c_fp]),
+    "psim_mlp_set_params": (ctypes.c_int, [ctypes.c_void_p, _c_fp]),
+    "psim_mlp_gradients": (ctypes.c_int, [ctypes.c_void_p, _c_fp, _c_fp, ctypes.c_int32, _c_fp, _c_fp]),
+    "psim_mlp_train": (ctypes.c_int, [ctypes.c_void_p, _c_fp, _c_fp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_float, ctypes.c_uint64, _c_fp]),
+    "psim_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, _c_fp, ctypes.c_int32, _c_fp]),
+    "psim_mlp_destroy": (None, [ctypes.c_void_p]),
     "psim_geom_intersect": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
@@ -236,6 +248,21 @@ class Model:
         out = ctypes.c_uint64()
         _check(lib().psim_model_steps_run(self._h, ctypes.byref(out)))
         return int(out.value)
+
+    def start_temps(self) -> np.ndarray:
+        """The temperature each sensor starts runs from (file order)."""
+        out = np.zeros(self.n_sensors)
+        _check(lib().psim_model_start_temps(self._h, _dp(out)))
+        return out
+
+    def set_start_temps(self, temps: Optional[np.ndarray]) -> None:
+        """Warm start: later runs start from these sensor temperatures (None: the file's)."""
+        if temps is None:
+            _check(lib().psim_model_set_start_temps(self._h, None))
+            return
+        t = np.ascontiguousarray(temps, dtype=np.float64)
+        assert t.shape == (self.n_sensors,)
+        _check(lib().psim_model_set_start_temps(self._h, _dp(t)))
 
     def measurements(self) -> np.ndarray:
         """[S, 6]: T, SE(T), flux x, SE, flux y, SE averaged over runs."""
@@ -367,6 +394,69 @@ def interpret(desc: InterpDesc, energy: np.ndarray, flux: np.ndarray):
     stats = np.zeros((S, 6))
     _check(lib().psim_interpret(ctypes.byref(desc), _i64(energy), _dp(flux), _dp(temps), _dp(fluxes), _dp(stats)))
     return temps, fluxes, stats
+
+
+def _f32(a: np.ndarray):
+    return a.ctypes.data_as(_c_fp)
+
+
+class Mlp:
+    """The warm-start surrogate's network on the GPU (psim_mlp_*): BF16 parameters and
+    activations, FP32 accumulation, GELU hidden layers, Adam."""
+
+    def __init__(self, widths, seed: int = 1):
+        w = np.ascontiguousarray(widths, dtype=np.int32)
+        self.widths = [int(v) for v in w]
+        self._h = ctypes.c_void_p()
+        _check(lib().psim_mlp_create(w.ctypes.data_as(_c_i32p), len(w), seed, ctypes.byref(self._h)))
+        n = ctypes.c_uint64()
+        _check(lib().psim_mlp_n_params(self._h, ctypes.byref(n)))
+        self.n_params = int(n.value)
+
+    def close(self) -> None:
+        if self._h:
+            lib().psim_mlp_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        _check(lib().psim_mlp_get_params(self._h, _f32(out)))
+        return out
+
+    @params.setter
+    def params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.shape == (self.n_params,)
+        _check(lib().psim_mlp_set_params(self._h, _f32(p)))
+
+    def gradients(self, x: np.ndarray, y: np.ndarray) -> Tuple[float, np.ndarray]:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = ctypes.c_float()
+        g = np.zeros(self.n_params, dtype=np.float32)
+        _check(lib().psim_mlp_gradients(self._h, _f32(x), _f32(y), len(x), ctypes.byref(loss), _f32(g)))
+        return float(loss.value), g
+
+    def train(self, x: np.ndarray, y: np.ndarray, batch: int = 256, epochs: int = 200, lr: float = 1e-3,
+              seed: int = 1) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(lib().psim_mlp_train(self._h, _f32(x), _f32(y), len(x), batch, epochs, lr, seed, ctypes.byref(loss)))
+        return float(loss.value)
+
+    def predict(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros((len(x), self.widths[-1]), dtype=np.float32)
+        _check(lib().psim_mlp_predict(self._h, _f32(x), len(x), _f32(y)))
+        return y
 
 
 def _handles(models):

@@ -10,6 +10,7 @@
 #include <string>
 
 #include "device/engine.hpp"
+#include "device/mlp.hpp"
 #include "host/batch.hpp"
 #include "host/model.hpp"
 
@@ -20,6 +21,10 @@ struct psim_model {
 
 struct psim_sim {
     std::unique_ptr<psim::gpu::Engine> e;
+};
+
+struct psim_mlp {
+    std::unique_ptr<psim::gpu::Mlp> net;
 };
 
 namespace {
@@ -153,6 +158,20 @@ int psim_model_population(const psim_model* m, uint32_t* out) {
     if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     if (m->m->engine() == nullptr) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
     return guard([&]() { m->m->engine()->population(out); });
+}
+
+int psim_model_start_temps(const psim_model* m, double* out) {
+    if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    const auto t = m->m->start_temps();
+    std::copy(t.begin(), t.end(), out);
+    return PSIM_OK;
+}
+
+int psim_model_set_start_temps(psim_model* m, const double* temps) {
+    if (m == nullptr) { return fail(PSIM_ERR_INVALID, "null model"); }
+    return guard([&]() {
+        m->m->set_start_temps(temps == nullptr ? std::vector<double>{} : std::vector<double>(temps, temps + m->m->n_sensors()));
+    });
 }
 
 int psim_model_export(const psim_model* m, const char* json_path, double seconds) {
@@ -452,6 +471,58 @@ int psim_sim_steps_run(const psim_sim* s, uint64_t* steps) {
     *steps = s->e->steps_run();
     return PSIM_OK;
 }
+
+// ------------------------------------------------------------------ the surrogate MLP
+int psim_mlp_create(const int32_t* widths, int32_t n_widths, uint64_t seed, psim_mlp** out) {
+    if (widths == nullptr || out == nullptr || n_widths < 2) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
+    return guard([&]() {
+        auto h = std::make_unique<psim_mlp>();
+        h->net = std::make_unique<psim::gpu::Mlp>(std::vector<int>(widths, widths + n_widths), seed);
+        *out = h.release();
+    });
+}
+
+int psim_mlp_n_params(const psim_mlp* net, uint64_t* n) {
+    if (net == nullptr || n == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    *n = net->net->n_params();
+    return PSIM_OK;
+}
+
+int psim_mlp_get_params(const psim_mlp* net, float* out) {
+    if (net == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    return guard([&]() { net->net->get_params(out); });
+}
+
+int psim_mlp_set_params(psim_mlp* net, const float* in) {
+    if (net == nullptr || in == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    return guard([&]() { net->net->set_params(in); });
+}
+
+int psim_mlp_gradients(psim_mlp* net, const float* x, const float* y, int32_t n, float* loss, float* grads) {
+    if (net == nullptr || x == nullptr || y == nullptr || n < 1) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
+    return guard([&]() {
+        const float l = net->net->gradients(x, y, n, grads);
+        if (loss != nullptr) { *loss = l; }
+    });
+}
+
+int psim_mlp_train(psim_mlp* net, const float* x, const float* y, int32_t n, int32_t batch, int32_t epochs, float lr, uint64_t seed,
+                   float* final_loss) {
+    if (net == nullptr || x == nullptr || y == nullptr || n < 1 || batch < 1 || epochs < 0 || !(lr > 0.f)) {
+        return fail(PSIM_ERR_INVALID, "bad arguments");
+    }
+    return guard([&]() {
+        const float l = net->net->train(x, y, n, batch, epochs, lr, seed);
+        if (final_loss != nullptr) { *final_loss = l; }
+    });
+}
+
+int psim_mlp_predict(psim_mlp* net, const float* x, int32_t n, float* y) {
+    if (net == nullptr || x == nullptr || y == nullptr || n < 0) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
+    return guard([&]() { net->net->predict(x, n, y); });
+}
+
+void psim_mlp_destroy(psim_mlp* net) { delete net; }
 
 // ------------------------------------------------------------------ batches of models
 namespace {

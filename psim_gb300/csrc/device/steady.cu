@@ -8,10 +8,12 @@
 //     batch means over sqrt(B) (batch means: a phonon stays in a sensor's cells for several
 //     steps, so per-step tallies are correlated and their own spread would understate the
 //     error);
-//   - window c "agrees" with window c-1 when, for every quantity, the means differ by at most
-//     z combined standard errors: |m_c - m_{c-1}| <= z sqrt(se_c^2 + se_{c-1}^2);
-//   - a sensor is steady from window j when each of the M windows after it agrees with its
-//     predecessor (M consecutive agreements); its onset is step j*W;
+//   - window c "agrees" with window j when, for every quantity, the means differ by at most
+//     z combined standard errors: |m_c - m_j| <= z sqrt(se_c^2 + se_j^2);
+//   - a sensor is steady from window j when each of the M windows after it agrees with window j
+//     itself (the anchor: a drift too slow to show between neighbouring windows still has to stay
+//     within the tolerance over all M of them); a window that disagrees becomes the next anchor;
+//     the onset is step j*W;
 //   - the model is steady at the largest onset over its sensors, and not steady while any
 //     sensor has none.
 // The statistics are computed in FP64 from the exact integer tallies (flux in fixed point), in a
@@ -51,6 +53,8 @@ __global__ void steady_kernel(const TallySlot* tally, std::uint32_t S, std::uint
     const std::uint32_t L = W / B;// steps per batch
     const std::uint64_t nw = k_used / W;
     WindowStats prev{};
+    WindowStats anchor{};
+    std::uint64_t anchor_w = 0;
     std::uint32_t streak = 0;
     long long result = -1;
     for (std::uint64_t w = 0; w < nw && result < 0; ++w) {
@@ -84,15 +88,18 @@ __global__ void steady_kernel(const TallySlot* tally, std::uint32_t S, std::uint
             cur.mean[q] = shift[q] + d;
             cur.se[q] = sqrt(var / n);
         }
-        if (w > 0) {
-            bool agree = true;
+        bool agree = w > 0;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const double tol = z * sqrt(cur.se[q] * cur.se[q] + prev.se[q] * prev.se[q]);
-                agree = agree && fabs(cur.mean[q] - prev.mean[q]) <= tol;
-            }
-            streak = agree ? streak + 1U : 0U;
-            if (streak >= M) { result = static_cast<long long>((w - M) * W); }
+        for (int q = 0; q < 3; ++q) {
+            const double tol = z * sqrt(cur.se[q] * cur.se[q] + anchor.se[q] * anchor.se[q]);
+            agree = agree && fabs(cur.mean[q] - anchor.mean[q]) <= tol;
+        }
+        if (agree) {
+            if (++streak >= M) { result = static_cast<long long>(anchor_w * W); }
+        } else {
+            anchor = cur;
+            anchor_w = w;
+            streak = 0;
         }
         prev = cur;
     }

@@ -331,13 +331,30 @@ std::unique_ptr<HostModel> HostModel::from_json(const std::string& path) {// Inp
     return m;
 }
 
+void HostModel::set_start_temps(const std::vector<double>& temps) {
+    if (!temps.empty() && temps.size() != sensors_.size()) { throw std::invalid_argument("one start temperature per sensor"); }
+    if (!temps.empty() && t_eq_ == 0.) { throw std::invalid_argument("start temperatures need a deviational model (t_eq > 0)"); }
+    for (double t : temps) {
+        if (!(t > 0.) || !std::isfinite(t)) { throw std::invalid_argument("start temperatures must be positive and finite"); }
+    }
+    t_start_ = temps;
+}
+
+std::vector<double> HostModel::start_temps() const {
+    std::vector<double> out;
+    for (std::size_t s = 0; s < sensors_.size(); ++s) { out.push_back(start_temp(s)); }
+    return out;
+}
+
 // ---------------------------------------------------------------- run orchestration
 double HostModel::init_temp(const SensorRec& s) const { return type_ == SimType::SteadyState ? s.t_steady : s.t_init; }
+
+double HostModel::start_temp(std::size_t s) const { return t_start_.empty() ? init_temp(sensors_[s]) : t_start_[s]; }
 
 double HostModel::cell_init_energy(std::size_t c) const {// Cell::getInitEnergy: cell.cpp:38-41
     const SensorRec& s = sensors_[cells_[c].sensor];
     const double e = cells_[c].area * s.heat_cap;
-    return (t_eq_ == 0.) ? e : e * std::fabs(init_temp(s) - t_eq_);
+    return (t_eq_ == 0.) ? e : e * std::fabs(start_temp(cells_[c].sensor) - t_eq_);
 }
 
 double HostModel::cell_emit_energy(std::size_t c) const {// Cell::getEmitEnergy: cell.cpp:45-63
@@ -478,7 +495,7 @@ gpu::InterpDesc HostModel::interp_desc(double eff) const {
     for (const auto& s : sensors_) {
         d.area.push_back(s.area);
         d.heat_capacity.push_back(s.heat_cap);
-        d.init_temp.push_back(init_temp(s));
+        d.init_temp.push_back(start_temp(static_cast<std::size_t>(&s - sensors_.data())));
         d.material.push_back(s.material);
     }
     d.mat_temp_begin.push_back(0);
@@ -564,7 +581,7 @@ std::vector<double> HostModel::emit_energies() const {// ModelSimulator::initPho
 
 std::vector<double> HostModel::sensor_init_temps() const {
     std::vector<double> out(sensors_.size());
-    for (std::size_t s = 0; s < sensors_.size(); ++s) { out[s] = init_temp(sensors_[s]); }
+    for (std::size_t s = 0; s < sensors_.size(); ++s) { out[s] = start_temp(s); }
     return out;
 }
 

@@ -90,6 +90,12 @@ public:
         stop_crit_ = c;
         stop_check_ = check_every;
     }
+    // Warm start (deviational models): the temperatures runs start from, per sensor in file
+    // order (an empty list restores the file's).  They set the cells' initial phonon energy and the first recorded
+    // temperature; the material tables and heat capacities stay at the file's t_init, so a warm
+    // run solves the same linearised problem as a cold one and reaches the same steady state.
+    void set_start_temps(const std::vector<double>& temps);
+    std::vector<double> start_temps() const;
     void run();// Model::runSimulation
     void export_results(const std::string& json_path, double seconds) const;
 
@@ -141,6 +147,7 @@ private:
     int precision_{ 0 };
     void* stream_{ nullptr };
     int grid_{ 0 };
+    std::vector<double> t_start_;// warm-start temperatures (empty: the file's)
     bool stop_on_{ false };
     gpu::SteadyCriterion stop_crit_{};
     std::uint64_t stop_check_{ 0 };
@@ -161,6 +168,7 @@ private:
 
     // run helpers
     double init_temp(const SensorRec& s) const;
+    double start_temp(std::size_t s) const;// the warm-start temperature, else init_temp
     double cell_init_energy(std::size_t c) const;
     double cell_emit_energy(std::size_t c) const;
     double total_energy() const;

@@ -228,19 +228,24 @@ def plate(*, length: float = 4000.0, width: float = 1000.0, nx: int = 64, ny: in
     return b.to_dict()
 
 
-def random_bar(seed: int, *, dt_ps: float = 5.0, steps: int = 3000, pilot_lifetime_steps: float = 100.0) -> Dict:
-    """One model of the batched workload, drawn from ``seed``: length U(0.2, 5) um,
-    width U(50, 500) nm, cells U{4..200}, phonons per step log-U(1e4, 1e6), end
-    temperatures U(280, 320) K, wall specularity U(0, 1).  The per-step population is
-    turned into psim's total phonon budget with a pilot mean lifetime in steps."""
+def random_bar_params(seed: int) -> Dict:
+    """The batched workload's parameters drawn from ``seed``: length U(0.2, 5) um, width
+    U(50, 500) nm, cells U{4..200}, phonons per step log-U(1e4, 1e6), end temperatures
+    U(280, 320) K, wall specularity U(0, 1)."""
     rng = random.Random(seed)
-    length = rng.uniform(200.0, 5000.0)
-    width = rng.uniform(50.0, 500.0)
-    cells = rng.randint(4, 200)
-    per_step = 10 ** rng.uniform(4.0, 6.0)
-    t_left, t_right = rng.uniform(280.0, 320.0), rng.uniform(280.0, 320.0)
-    spec = rng.uniform(0.0, 1.0)
-    budget = int(per_step * steps / pilot_lifetime_steps)
-    return bar(num_cells=cells, length=length, width=width, t_left=t_left, t_right=t_right, t_init=300.0,
-               t_eq=300.0, spec=spec, num_measurements=steps, sim_time=steps * dt_ps * 1e-3,
-               num_phonons=max(budget, 1000))
+    return {"length": rng.uniform(200.0, 5000.0), "width": rng.uniform(50.0, 500.0), "cells": rng.randint(4, 200),
+            "per_step": 10 ** rng.uniform(4.0, 6.0), "t_left": rng.uniform(280.0, 320.0),
+            "t_right": rng.uniform(280.0, 320.0), "spec": rng.uniform(0.0, 1.0)}
+
+
+def random_bar(seed: int, *, dt_ps: float = 5.0, steps: int = 3000, pilot_lifetime_steps: float = 100.0,
+               periodic: bool = False, per_step_scale: float = 1.0) -> Dict:
+    """One model of the batched workload (``random_bar_params``).  The per-step population is
+    turned into psim's total phonon budget with a pilot mean lifetime in steps.  Steady-state
+    mode by default; ``periodic`` records every step (output every 50 steps) for measuring the
+    time to steady state."""
+    q = random_bar_params(seed)
+    budget = int(q["per_step"] * per_step_scale * steps / pilot_lifetime_steps)
+    return bar(num_cells=q["cells"], length=q["length"], width=q["width"], t_left=q["t_left"], t_right=q["t_right"],
+               t_init=300.0, t_eq=300.0, spec=q["spec"], num_measurements=steps, sim_time=steps * dt_ps * 1e-3,
+               num_phonons=max(budget, 1000), sim_type=1 if periodic else 0, step_interval=50 if periodic else 0)

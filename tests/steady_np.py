@@ -3,8 +3,9 @@
 Windows of W recorded steps per sensor over (energy count, flux x, flux y), flux in fixed point
 (2^20 units per m/s), each window split into B batches of W/B steps; a window's mean is the mean
 of its batch means and its standard error their spread over sqrt(B) (sums about the previous
-window's mean); window c agrees with c-1 when |m_c - m_{c-1}| <= z sqrt(se_c^2 + se_{c-1}^2) for
-all three; a sensor's onset is j*W for the first j followed by M agreeing windows; the model's
+window's mean); window c agrees with the anchor window j when |m_c - m_j| <= z sqrt(se_c^2 +
+se_j^2) for all three, and a window that disagrees becomes the anchor (window 0 is the first);
+a sensor's onset is j*W for the first anchor j followed by M agreeing windows; the model's
 onset is the largest over the sensors, -1 when any sensor has none."""
 import numpy as np
 
@@ -23,7 +24,9 @@ def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: in
     for s in range(S):
         series = [energy[s].astype(np.float64), fx[s], fy[s]]
         prev_mean = np.zeros(3)
-        prev_se = np.zeros(3)
+        anchor_mean = np.zeros(3)
+        anchor_se = np.zeros(3)
+        anchor_w = 0
         streak = 0
         for w in range(nw):
             mean = np.zeros(3)
@@ -35,13 +38,15 @@ def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: in
                 var = max(0.0, (np.sum(bm * bm) - batches * d * d) / (batches - 1))
                 mean[q] = prev_mean[q] + d
                 se[q] = np.sqrt(var / batches)
-            if w > 0:
-                agree = bool(np.all(np.abs(mean - prev_mean) <= z * np.sqrt(se * se + prev_se * prev_se)))
-                streak = streak + 1 if agree else 0
+            agree = w > 0 and bool(np.all(np.abs(mean - anchor_mean) <= z * np.sqrt(se * se + anchor_se * anchor_se)))
+            if agree:
+                streak += 1
                 if streak >= patience:
-                    out[s] = (w - patience) * window
+                    out[s] = anchor_w * window
                     break
-            prev_mean, prev_se = mean, se
+            else:
+                anchor_mean, anchor_se, anchor_w, streak = mean, se, w, 0
+            prev_mean = mean
     return out
 
 

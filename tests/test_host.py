@@ -234,3 +234,23 @@ def test_modelgen_workloads_load(api):
         assert d.n_emitters == 6
         p = api.Model(mg.write(mg.plate(num_phonons=1000), os.path.join(td, "p.json")))
         assert p.n_sensors == 1024 and p.n_cells == 2048 and p.sim_desc().n_emitters == 4
+
+
+def test_start_temperatures_are_checked_and_reset(api):
+    m = api.Model(model_path("bar_periodic"))
+    t0 = m.start_temps()
+    assert t0.shape == (m.n_sensors,) and np.all(t0 > 0)
+    warm = np.linspace(305.0, 295.0, m.n_sensors)
+    m.set_start_temps(warm)
+    assert np.array_equal(m.start_temps(), warm)
+    m.set_start_temps(None)
+    assert np.array_equal(m.start_temps(), t0)
+    bad = warm.copy()
+    bad[1] = -1.0
+    with pytest.raises(api.PsimError) as e:
+        m.set_start_temps(bad)
+    assert e.value.code == api.PSIM_ERR_INVALID
+    full = api.Model(model_path("bar_full"))
+    with pytest.raises(api.PsimError) as e:
+        full.set_start_temps(np.full(full.n_sensors, 50.0))
+    assert e.value.code == api.PSIM_ERR_INVALID

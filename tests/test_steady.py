@@ -35,6 +35,23 @@ def test_restatement_finds_the_plateau():
     assert model_onset(sensor_onsets(drift, flux, 50, 5, 3.0, 3)) == -1
 
 
+def drifting_series(seed: int, rate: float = 0.3, K: int = 1500, level: float = 400.0):
+    """Counts that keep rising by `rate` per step: 15 per 50-step window, about two standard
+    errors of a window mean, so neighbouring windows agree while the drift over three does not."""
+    rng = np.random.default_rng(seed)
+    energy = rng.poisson(level + rate * np.arange(K), size=(1, K)).astype(np.int64)
+    return energy, np.zeros((1, K, 2))
+
+
+def test_restatement_sees_a_slow_drift():
+    for seed in range(10):
+        energy, flux = drifting_series(seed)
+        assert model_onset(sensor_onsets(energy, flux, 50, 5, 3.0, 3)) == -1, seed
+    # and a flat series with the same noise is steady from the start
+    energy, flux = drifting_series(0, rate=0.0)
+    assert model_onset(sensor_onsets(energy, flux, 50, 5, 3.0, 3)) == 0
+
+
 def test_arguments_are_checked(built):
     from psim_gb300 import api
     e = np.zeros((2, 100), dtype=np.int64)
@@ -55,6 +72,16 @@ def test_gpu_matches_restatement_on_synthetic_series(gpu, seed, window, batches,
     want = sensor_onsets(energy, flux, window, batches, 3.0, patience)
     assert np.array_equal(per, want)
     assert onset == model_onset(want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed,rate", [(0, 0.3), (1, 0.16), (2, 0.0)])
+def test_gpu_matches_restatement_on_drifting_series(gpu, seed, rate):
+    from psim_gb300 import api
+    energy, flux = drifting_series(seed, rate)
+    onset, per = api.steady_state(energy, flux, window=50, batches=5, z=3.0, patience=3)
+    want = sensor_onsets(energy, flux, 50, 5, 3.0, 3)
+    assert np.array_equal(per, want) and onset == model_onset(want)
 
 
 @pytest.mark.gpu
