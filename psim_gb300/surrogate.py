@@ -221,6 +221,7 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
         "steps_ratio_cold_over_warm": float(cold_on.mean() / max(warm_on.mean(), 1.0)),
         "median_ratio_where_both_steady": float(np.median(cold_on[both] / np.maximum(warm_on[both], window)))
         if both.any() else None,
+        "steady_in_both": int(both.sum()),
         "never_steady_cold": int(sum(r["cold"] < 0 for r in rows)),
         "never_steady_warm": int(sum(r["warm"] < 0 for r in rows)),
         "detector": f"windows of {window} steps ({batches} batch means) within 3 SE of the run's anchor window for "
