@@ -12,6 +12,13 @@ Phonon-steps are counted by the kernels (phonons alive at a measurement boundary
 so the budget is num_phonons = 1e7 * steps / L with L the mean lifetime in steps measured
 by an untimed pilot run of the same model.
 
+Outside the timed region the line also carries:
+  batch       256 independent random rectangles run concurrently (autotuned workers and grid)
+  warm_start  time to steady state (3 SE, against an independent longer run) of held-out
+              rectangles started from the GPU-trained surrogate's temperatures vs the plain
+              cold start
+  fp32_vs_fp64  the FP32 kernel's error against the FP64 kernel on the same random streams
+
 --impl reference times the CPU oracle (the reference algorithm restated in C++, bit-exact
 with the reference on the same seed) on a bounded sample of the same model with every host
 thread.  Under torchrun each rank simulates its own phonons (weak scaling: the rank's seed
@@ -37,6 +44,7 @@ PER_STEP = 1.0e7
 STEPS = 5000
 DT_PS = 2.0
 BYTES_PER_PHONON_STEP = 64  # one 32-byte state record read and one written
+BATCH_CHUNK = 64  # batched models alive at once
 
 
 def dist_env():
@@ -186,8 +194,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP32-vs-FP64 same-stream comparison")
-    ap.add_argument("--batch-models", type=int, default=64,
+    ap.add_argument("--batch-models", type=int, default=256,
                     help="models of the batched workload (random rectangles) to time concurrently; 0 skips it")
+    ap.add_argument("--warm-start-train", type=int, default=512,
+                    help="training fields of the warm-start surrogate (0 skips the warm-start measurement)")
+    ap.add_argument("--warm-start-test", type=int, default=16, help="held-out rectangles of the warm-start measurement")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -322,27 +333,64 @@ def main():
                       "seed_to_seed_sd_K": float(noise), "mean_diff_over_sd": float(diff.mean() / noise)}
 
     # the batched workload: independent random rectangles (uneven cells and populations) run
-    # concurrently, options from the autotuner, against the same models one at a time
+    # concurrently, options from the autotuner, in chunks of BATCH_CHUNK models alive at once
+    # (each model keeps device buffers sized for its run's phonons); the first chunk also runs
+    # one model at a time for comparison
     batch = None
     if rank == 0 and world == 1 and args.batch_models > 0:
         from psim_gb300 import modelgen as mg
-        paths = [mg.write(mg.random_bar(1000 + i), os.path.join(td, f"rect_{i}.json")) for i in range(args.batch_models)]
-        models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in enumerate(paths)]
-        opt, tuned_rate = api.batch_autotune(models, sample=min(8, len(models)))
-        secs, steps_b = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
-        t0 = time.perf_counter()
-        steps_s = 0
-        for i, m in enumerate(models):
-            m.run(seed=i + 1, precision=precision)
-            steps_s += m.counters()["phonon_steps"]
-        secs_s = time.perf_counter() - t0
-        batch = {"workload": f"{len(models)} random rectangles: length U(0.2, 5) um, width U(50, 500) nm, 4-200 cells, "
+        opt = None
+        secs = 0.0
+        steps_b = 0
+        single = None
+        for c0 in range(0, args.batch_models, BATCH_CHUNK):
+            ids = range(c0, min(c0 + BATCH_CHUNK, args.batch_models))
+            paths = [mg.write(mg.random_bar(1000 + i), os.path.join(td, f"rect_{i}.json")) for i in ids]
+            models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in zip(ids, paths)]
+            if opt is None:
+                opt, tuned_rate = api.batch_autotune(models, sample=min(8, len(models)))
+            s_c, n_c = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
+            secs += s_c
+            steps_b += n_c
+            if single is None:
+                t0 = time.perf_counter()
+                steps_s = 0
+                for i, m in zip(ids, models):
+                    m.run(seed=i + 1, precision=precision)
+                    steps_s += m.counters()["phonon_steps"]
+                secs_s = time.perf_counter() - t0
+                single = {"models": len(models), "value": steps_s / secs_s, "seconds": secs_s,
+                          "batched_value": n_c / s_c}
+            for m in models:
+                m.close()
+        batch = {"workload": f"{args.batch_models} random rectangles: length U(0.2, 5) um, width U(50, 500) nm, 4-200 cells, "
                              "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
-                             "3000 steps of 5 ps, steady state",
+                             f"3000 steps of 5 ps, steady state; run {BATCH_CHUNK} at a time",
                  "autotuned": {"workers": opt.workers, "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate,
-                               "pilot_models": min(8, len(models))},
+                               "pilot_models": 8},
                  "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
-                 "one_at_a_time": {"value": steps_s / secs_s, "seconds": secs_s}}
+                 "one_at_a_time": single}
+
+    # the learned warm start: a surrogate trained on GPU Monte Carlo steady fields (outside the
+    # timed region), held-out rectangles run cold and warm, each timed to steady state at 3 SE
+    # against an independent run twice as long
+    warm = None
+    if rank == 0 and world == 1 and args.warm_start_train > 0 and precision == api.FP32:
+        from psim_gb300 import surrogate as sg
+        t0 = time.perf_counter()
+        X, Y = sg.generate(range(10000, 10000 + args.warm_start_train))
+        t_gen = time.perf_counter() - t0
+        net, loss = sg.train(X, Y)
+        held = sg.held_out(args.warm_start_test)
+        Xt, Yt = sg.generate(held)
+        test_rmse = float(np.sqrt(np.mean((net.predict(Xt) - Yt) ** 2)) * sg.T_SCALE)
+        rep = sg.summary(sg.evaluate(net, held, steps=6000))
+        net.close()
+        warm = {"workload": f"surrogate (12 -> 4 x 256 GELU -> 32 x 32, BF16 with FP32 sums) trained 200 epochs on "
+                            f"{args.warm_start_train} steady fields of random rectangles; {len(held)} held-out rectangles "
+                            "up to 2 um, 6000 steps of 5 ps, every step recorded",
+                "train_fields_s": t_gen, "final_train_loss": loss, "test_rmse_K": test_rmse}
+        warm.update(rep)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -367,6 +415,7 @@ def main():
                        "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
             "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check, "batch": batch,
+            "warm_start": warm,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

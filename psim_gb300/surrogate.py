@@ -239,6 +239,18 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
     }
 
 
+def held_out(n: int, max_length: float = 2000.0) -> List[int]:
+    """Seeds of ``n`` held-out rectangles (seeds from 50000, disjoint from the training seeds)
+    no longer than ``max_length`` nm: diffusion time <= ~12 ns at 2 um, so a cold start settles
+    within the evaluation runs and the two final states can be compared."""
+    return [k for k in range(50000, 60000) if mg.random_bar_params(k)["length"] <= max_length][:n]
+
+
+def summary(report: Dict) -> Dict:
+    """The evaluation without its per-model rows."""
+    return {k: v for k, v in report.items() if k != "per_model"}
+
+
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2048, help="training rectangles")
@@ -256,9 +268,7 @@ def main(argv=None) -> int:
     t0 = time.perf_counter()
     net, loss = train(X, Y, epochs=args.epochs)
     t_train = time.perf_counter() - t0
-    # held-out rectangles short enough (<= 2 um: diffusion time <= ~12 ns) for a cold start to
-    # settle within the evaluation runs, so that the two final states can be compared
-    held = [k for k in range(50000, 60000) if mg.random_bar_params(k)["length"] <= args.max_eval_length][:args.test]
+    held = held_out(args.test, args.max_eval_length)
     Xt, Yt = generate(held, steps=args.steps, scale=args.scale)
     test_mse = float(np.mean((net.predict(Xt) - Yt) ** 2))
     report = {"train_models": args.train, "epochs": args.epochs, "final_train_loss": loss,
