@@ -196,9 +196,9 @@ def main():
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP32-vs-FP64 same-stream comparison")
     ap.add_argument("--batch-models", type=int, default=256,
                     help="models of the batched workload (random rectangles) to time concurrently; 0 skips it")
-    ap.add_argument("--warm-start-train", type=int, default=512,
+    ap.add_argument("--warm-start-train", type=int, default=1024,
                     help="training fields of the warm-start surrogate (0 skips the warm-start measurement)")
-    ap.add_argument("--warm-start-test", type=int, default=16, help="held-out rectangles of the warm-start measurement")
+    ap.add_argument("--warm-start-test", type=int, default=32, help="held-out rectangles of the warm-start measurement")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":

@@ -145,6 +145,23 @@ def onset_vs_reference(temps: np.ndarray, t_inf: np.ndarray, spread: np.ndarray,
     return int(bad[-1] + 1) * window
 
 
+def stopped_within(m: api.Model, ref: Tuple[np.ndarray, np.ndarray, int], window: int, batches: int,
+                   patience: int) -> bool:
+    """Whether a run stopped by the steady-state detector ends on the steady state at 3 SE: each
+    sensor's mean temperature from the detector's onset to the stop lies within the prediction
+    bound of the reference's steady temperature.  The bound scales the spread of one window mean
+    to the averaged length (sd x sqrt(window / steps), windows taken as independent) and is
+    family-wise over the sensors (Student's t on the reference's degrees of freedom)."""
+    temps, _ = m.series(0)
+    onset, _ = m.steady_state(window=window, batches=batches, patience=patience)
+    k = temps.shape[1]
+    start = onset if 0 <= onset < k else max(k - window, 0)
+    mean = temps[:, start:].mean(axis=1)
+    t_inf, spread, dof = ref
+    se = np.sqrt(spread * spread * window / max(k - start, 1))
+    return bool(np.all(np.abs(mean - t_inf) <= _bound(len(t_inf), dof) * se))
+
+
 def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: float = 1.0, window: int = 100,
              batches: int = 5, patience: int = 3, workers: int = 16) -> Dict:
     """Cold and warm starts of the rectangles drawn from ``seeds``.
@@ -153,7 +170,8 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
     temperatures and their window tolerance (``steady_reference``).  The cold and warm runs (every
     step recorded) are timed to steady state against it (``onset_vs_reference``: at 3 SE) and by
     the run's own detector; then the same runs again with the steady stop on give the wall time
-    and steps a batch of them takes to stop at steady state."""
+    and steps a batch of them takes to stop at steady state, and whether each stopped run's
+    result lies within 3 SE of the steady state (``stopped_within``)."""
     seeds = list(seeds)
     rows = []
     t_cold = t_warm = 0.0
@@ -200,9 +218,11 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
             t0 = time.perf_counter()
             api.batch_run([m for m, _ in warm], workers=workers)
             ts_warm += time.perf_counter() - t0
-            for r, (mc, _), (mw, _) in zip(rows[len(rows) - len(chunk):], cold, warm):
+            for r, (mc, _), (mw, _), ref_k in zip(rows[len(rows) - len(chunk):], cold, warm, refs):
                 r["cold_stop"] = mc.steps_run()
                 r["warm_stop"] = mw.steps_run()
+                r["cold_stop_ok"] = stopped_within(mc, ref_k, window, batches, patience)
+                r["warm_stop_ok"] = stopped_within(mw, ref_k, window, batches, patience)
                 mc.close()
                 mw.close()
 
@@ -235,6 +255,8 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
         "wall_ratio_cold_over_warm_to_steady_stop": ts_cold / max(ts_warm, 1e-9),
         "mean_steps_run_cold_to_steady_stop": float(np.mean([r["cold_stop"] for r in rows])),
         "mean_steps_run_warm_to_steady_stop": float(np.mean([r["warm_stop"] for r in rows])),
+        "stopped_within_3se_cold": float(np.mean([r["cold_stop_ok"] for r in rows])),
+        "stopped_within_3se_warm": float(np.mean([r["warm_stop_ok"] for r in rows])),
         "per_model": rows,
     }
 

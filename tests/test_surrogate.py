@@ -33,6 +33,33 @@ def test_onset_against_a_reference():
     assert sg.onset_vs_reference(steady + 1.0, *ref, W) == -1
 
 
+class _StoppedRun:
+    """A run stopped by the detector, as stopped_within sees it: its recorded temperatures and
+    the detector's onset."""
+
+    def __init__(self, temps, onset):
+        self.temps, self.onset = temps, onset
+
+    def series(self, run=0):
+        return self.temps, None
+
+    def steady_state(self, **kw):
+        return self.onset, None
+
+
+def test_stopped_run_accuracy():
+    from psim_gb300 import surrogate as sg
+    rng = np.random.default_rng(5)
+    t_inf = np.array([300.0, 305.0, 310.0])
+    ref = sg.steady_reference(t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 4000)), 50)
+    steady = t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 600))
+    assert sg.stopped_within(_StoppedRun(steady, 200), ref, 50, 5, 3)
+    # stopped while still a kelvin away: the mean over the certified part misses the bound
+    assert not sg.stopped_within(_StoppedRun(steady - 1.0, 200), ref, 50, 5, 3)
+    # no onset: the last window is taken
+    assert sg.stopped_within(_StoppedRun(steady, -1), ref, 50, 5, 3)
+
+
 @pytest.mark.gpu
 def test_warm_start_reaches_the_steady_state_sooner(gpu, tmp_path):
     """A 300 nm bar (diffusion time ~0.3 ns) run for 5 ns: cold, then warm from the cold run's
