@@ -18,6 +18,8 @@ Outside the timed region the line also carries:
               rectangles started from the GPU-trained surrogate's temperatures vs the plain
               cold start
   fp32_vs_fp64  the FP32 kernel's error against the FP64 kernel on the same random streams
+  other_workloads  the steady-state bar, its full-mode twin and the transient plate, each
+              with its device and end-to-end rates beside the CPU oracle
 
 --impl reference times the CPU oracle (the reference algorithm restated in C++, bit-exact
 with the reference on the same seed) on a bounded sample of the same model with every host
@@ -147,6 +149,59 @@ def cpu_sample(path_dir: str, budget: int, threads: int, seed: int):
     return r.phonon_steps, r.seconds
 
 
+def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
+    """The other single-model workloads, untimed by the headline: per model the device rate
+    (phonon-steps / transport-kernel time), the end-to-end rate of psim_model_run (host wall
+    time of the call) and, where ``cpu``, the CPU oracle on ``threads`` host threads (the whole
+    workload, or a bounded sample of it where stated).  Per-step populations become psim's
+    phonon budgets through a pilot run's mean lifetime, as for the kinked model."""
+    from psim_gb300 import api, modelgen as mg
+
+    def budget(make, per_step, steps):
+        pilot = api.Model(mg.write(make(200000), os.path.join(td, "pilot_w.json")))
+        pilot.run(seed=3, precision=precision)
+        c = pilot.counters()
+        pilot.close()
+        return int(per_step * steps / max(c["phonon_steps"] / max(c["phonons"], 1), 1.0))
+
+    bar0 = lambda n: mg.bar(num_cells=10, length=1000.0, width=100.0, t_left=310.0, t_right=290.0, t_init=300.0,
+                            t_eq=300.0, num_measurements=2000, sim_time=10.0, num_phonons=n)
+    full = lambda n: mg.bar(num_cells=10, length=1000.0, width=100.0, t_left=60.0, t_right=40.0, t_init=50.0,
+                            t_eq=0.0, num_measurements=2000, sim_time=10.0, num_phonons=n)
+    n0 = budget(bar0, 2e5, 2000)
+    cases = [
+        ("bar_steady_state", "1000 x 100 nm bar, 10 cells, deviational steady state, ends 310/290 K, 2e5 phonons per "
+                             "step, dt 5 ps, 2000 steps", bar0(n0), bar0(n0 // 4)),
+        ("bar_full_mode", "the same bar in full (non-deviational) mode, ends 60/40 K, 2e5 phonons per step, dt 5 ps, "
+                          "2000 steps", full(budget(full, 2e5, 2000)), None),
+        ("plate_transient", "4 x 1 um plate, 64 x 16 cells, transient, 400 K pulse on a 200 nm strip of the left edge "
+                            "for 20 ps, 2e7 phonons, dt 1 ps, 3000 steps", mg.plate(), mg.plate(num_phonons=100000)),
+    ]
+    out = {}
+    for key, text, model, sample in cases:
+        path = mg.write(model, os.path.join(td, key + ".json"))
+        m = api.Model(path)
+        m.run(seed=1, precision=precision)  # warm-up: tables, graph
+        t0 = time.perf_counter()
+        m.run(seed=2, precision=precision)
+        m.measurements()
+        wall = time.perf_counter() - t0
+        c = m.counters()
+        m.close()
+        row = {"workload": text, "num_phonons": model["settings"]["num_phonons"], "phonon_steps": c["phonon_steps"],
+               "value": c["phonon_steps"] / (c["kernel_ms"] / 1e3), "e2e": c["phonon_steps"] / wall,
+               "unit": "phonon-steps/s", "mean_population": c["phonon_steps"] / model["settings"]["num_measurements"]}
+        if cpu:
+            from oracle import oracle
+            cpath = path if sample is None else mg.write(sample, os.path.join(td, key + "_sample.json"))
+            r = oracle.run(cpath, 5, threads=threads)
+            row["cpu_oracle"] = {"value": r.phonon_steps / r.seconds, "cores": threads, "seconds": r.seconds,
+                                 "sample": "the whole workload" if sample is None else
+                                 f"the same model with a {sample['settings']['num_phonons']}-phonon budget"}
+        out[key] = row
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference algorithm (CPU oracle) on every host thread."""
     if rank != 0:
@@ -193,6 +248,7 @@ def main():
     ap.add_argument("--population-out", default="", help="write the phonon population per step of the last timed run (JSON)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-others", action="store_true", help="skip the other single-model workloads")
     ap.add_argument("--no-fp64-check", action="store_true", help="skip the FP32-vs-FP64 same-stream comparison")
     ap.add_argument("--batch-models", type=int, default=256,
                     help="models of the batched workload (random rectangles) to time concurrently; 0 skips it")
@@ -392,6 +448,10 @@ def main():
                 "train_fields_s": t_gen, "final_train_loss": loss, "test_rmse_K": test_rmse}
         warm.update(rep)
 
+    others = None
+    if rank == 0 and world == 1 and not args.no_others:
+        others = other_workloads(td, precision, os.cpu_count() or 1, not args.no_cpu)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -415,7 +475,7 @@ def main():
                        "steps_per_launch": c["steps_per_launch"]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
             "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check, "batch": batch,
-            "warm_start": warm,
+            "warm_start": warm, "other_workloads": others,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

