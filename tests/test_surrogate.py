@@ -53,11 +53,13 @@ def test_stopped_run_accuracy():
     t_inf = np.array([300.0, 305.0, 310.0])
     ref = sg.steady_reference(t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 4000)), 50)
     steady = t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 600))
-    assert sg.stopped_within(_StoppedRun(steady, 200), ref, 50, 5, 3)
-    # stopped while still a kelvin away: the mean over the certified part misses the bound
-    assert not sg.stopped_within(_StoppedRun(steady - 1.0, 200), ref, 50, 5, 3)
+    assert sg.stopped_within(_StoppedRun(steady, 200), ref, 50, 5, 3) == (True, True)
+    # stopped while still a kelvin away: both standards miss
+    assert sg.stopped_within(_StoppedRun(steady - 1.0, 200), ref, 50, 5, 3) == (False, False)
+    # a tenth of a kelvin off: inside one window's bound, outside the bound of a 400-step mean
+    assert sg.stopped_within(_StoppedRun(steady - 0.1, 200), ref, 50, 5, 3) == (True, False)
     # no onset: the last window is taken
-    assert sg.stopped_within(_StoppedRun(steady, -1), ref, 50, 5, 3)
+    assert sg.stopped_within(_StoppedRun(steady, -1), ref, 50, 5, 3) == (True, True)
 
 
 @pytest.mark.gpu
