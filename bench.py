@@ -140,11 +140,11 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(path_dir: str, budget: int, threads: int, seed: int):
+def cpu_sample(path_dir: str, budget: int, threads: int, seed: int, steps: int = STEPS, dt_ps: float = DT_PS):
     """The oracle on a bounded sample of the workload (same model, smaller phonon budget)."""
     from oracle import oracle
     oracle.build()
-    p = model_json(os.path.join(path_dir, "kinked_sample.json"), budget)
+    p = model_json(os.path.join(path_dir, "kinked_sample.json"), budget, steps, dt_ps)
     r = oracle.run(p, seed, threads=threads)
     return r.phonon_steps, r.seconds
 
@@ -202,6 +202,11 @@ def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
     return out
 
 
+def workload_name(args) -> str:
+    return (f"kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt {args.dt_ps:g} ps, "
+            f"{args.measurements} steps, output every 50 steps, {args.per_step:.0e} phonons per step")
+
+
 def run_reference(args, rank, world):
     """--impl reference: the reference algorithm (CPU oracle) on every host thread."""
     if rank != 0:
@@ -210,11 +215,11 @@ def run_reference(args, rank, world):
     budget = args.cpu_budget
     with tempfile.TemporaryDirectory() as td:
         for _ in range(args.warmup):
-            cpu_sample(td, budget, threads, 7)
+            cpu_sample(td, budget, threads, 7, args.measurements, args.dt_ps)
         steps = 0
         secs = 0.0
         for k in range(args.steps):
-            n, s = cpu_sample(td, budget, threads, 100 + k)
+            n, s = cpu_sample(td, budget, threads, 100 + k, args.measurements, args.dt_ps)
             steps += n
             secs += s
     rate = steps / secs
@@ -222,10 +227,10 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": "phonon-steps/s", "value": rate, "unit": "phonon-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "kinked 3-arm, 400 cells/sensors, periodic, dt 2 ps, 5000 steps",
-                   "num_phonons": budget, "sample": f"budget {budget} phonons (bounded CPU sample)"},
+        "config": {"workload": workload_name(args), "num_phonons": budget,
+                   "sample": f"budget {budget} phonons per run (a bounded CPU sample of the same model)"},
         "cpu_baseline": {"value": rate, "unit": "phonon-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"kinked model, 5000 steps, {budget}-phonon budget per run, on {threads} host threads; "
+                         "sample": f"kinked model, {args.measurements} steps, {budget}-phonon budget per run, on {threads} host threads; "
                                    "the reference built from its sources (oracle/_ref) cannot be built without them, so "
                                    "the bit-exact C++ restatement of its algorithm (oracle/) runs"},
         "e2e": {"value": rate, "unit": "phonon-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -460,7 +465,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        n, s = cpu_sample(td, args.cpu_budget, threads, 5)
+        n, s = cpu_sample(td, args.cpu_budget, threads, 5, steps_n, args.dt_ps)
         cpu = {"value": n / s, "unit": "phonon-steps/s", "cores": threads, "kind": "port",
                "sample": f"kinked model, {steps_n} steps, {args.cpu_budget}-phonon budget ({n} phonon-steps, {s:.1f} s) "
                          f"on {threads} host threads with the CPU oracle"}
@@ -471,8 +476,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if precision == api.FP32 else "f64",
             "data": "synthetic",
-            "config": {"workload": f"kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt {args.dt_ps:g} ps, "
-                                   f"{steps_n} steps, output every 50 steps, {args.per_step:.0e} phonons per step",
+            "config": {"workload": workload_name(args),
                        "num_phonons_per_rank": budget, "mean_lifetime_steps": lifetime,
                        "mean_population": phonon_steps / args.steps / steps_n,
                        "l2": "inputs larger than L2 (phonon state 2 x 32 B x population)",
