@@ -16,6 +16,24 @@ def test_raster_round_trip():
     assert sg.features(q).shape == (sg.FEATURES,)
 
 
+def test_workload_draws():
+    """The random rectangles follow their stated distribution, and the held-out set is short
+    enough to settle and disjoint from the training seeds."""
+    from psim_gb300 import modelgen as mg
+    from psim_gb300 import surrogate as sg
+    qs = [mg.random_bar_params(k) for k in range(2000)]
+    for q in qs:
+        assert 200.0 <= q["length"] <= 5000.0 and 50.0 <= q["width"] <= 500.0 and 4 <= q["cells"] <= 200
+        assert 1e4 <= q["per_step"] <= 1e6 and 280.0 <= q["t_left"] <= 320.0 and 280.0 <= q["t_right"] <= 320.0
+        assert 0.0 <= q["spec"] <= 1.0
+    # log-uniform populations: about half of the draws below 1e5
+    assert 0.45 < np.mean([q["per_step"] < 1e5 for q in qs]) < 0.55
+    held = sg.held_out(64)
+    assert len(held) == 64 and len(set(held)) == 64 and min(held) >= 50000
+    assert all(mg.random_bar_params(k)["length"] <= 2000.0 for k in held)
+    assert held == sg.held_out(64)
+
+
 def test_onset_against_a_reference():
     from psim_gb300 import surrogate as sg
     rng = np.random.default_rng(3)
