@@ -34,3 +34,14 @@ def gpu(built):
 
 def model_path(name: str) -> str:
     return os.path.join(GOLDEN, "models", name + ".json")
+
+
+def demo_model_path(name: str, directory: str) -> str:
+    """One of the reference's own demo models (tests/golden/models/<name>.json.gz), written
+    out as plain JSON into ``directory``."""
+    import gzip
+    out = os.path.join(directory, name + ".json")
+    if not os.path.exists(out):
+        with gzip.open(os.path.join(GOLDEN, "models", name + ".json.gz"), "rb") as f, open(out, "wb") as g:
+            g.write(f.read())
+    return out

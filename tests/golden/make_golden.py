@@ -11,10 +11,14 @@ Outputs (all small):
   tables_<model>.npz     material tables after Model::initializeMaterialTables
   invert_<model>.npz     SensorInterpreter results for given tallies
   runs_<model>.npz       per-sensor results of 16 seeded reference runs (statistical parity)
+  models/<demo>.json.gz  the reference's own demo models (psim_python/json/), gzipped, and
+  runs_<demo>.npz        16 seeded runs of each by the reference built from its sources, with
+                         the result table the reference commits for it (psim_python/json/results/)
 """
 from __future__ import annotations
 
 import argparse
+import gzip
 import json
 import os
 import subprocess
@@ -247,6 +251,41 @@ def make_runs(paths, names):
         print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}")
 
 
+# ---------------------------------------------------------------- the reference's own demo models
+DEMOS = ["linear_demo", "linear_sides_demo_ss", "kinked_demo_120_35_spec"]
+
+
+def copy_demos(reference):
+    """The demo model files the reference ships, gzipped into models/; returns plain copies in a
+    temporary directory for the reference driver."""
+    td = tempfile.mkdtemp(prefix="psim_demos_")
+    paths = {}
+    for name in DEMOS:
+        src = os.path.join(reference, "psim_python", "json", name + ".json")
+        data = open(src, "rb").read()
+        with gzip.GzipFile(os.path.join(MODELS, name + ".json.gz"), "wb", mtime=0) as f:
+            f.write(data)
+        paths[name] = os.path.join(td, name + ".json")
+        with open(paths[name], "wb") as f:
+            f.write(data)
+    return paths
+
+
+def make_demo_runs(reference, paths):
+    """16 seeded reference runs of each demo, next to the steady-state table the reference
+    commits for it (a single unseeded run: T, SE, flux x, SE, flux y, SE per sensor)."""
+    for name in DEMOS:
+        committed = np.loadtxt(os.path.join(reference, "psim_python", "json", "results", f"ss_{name}.txt"), skiprows=1)
+        with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
+            res = list(pool.map(lambda s: ref_run(paths[name], s), SEEDS))
+        stats = np.stack([r[0] for r in res])
+        phonons = np.array([r[1] for r in res])
+        # float32 keeps these larger tables small; seed-to-seed spreads are far above its resolution
+        np.savez_compressed(os.path.join(HERE, f"runs_{name}.npz"), seeds=np.array(SEEDS), stats=stats.astype(np.float32),
+                            phonons=phonons, committed=committed.astype(np.float32))
+        print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}, committed {committed[:4, 0]}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -266,6 +305,8 @@ def main():
         make_invert(paths)
     if not args.skip_runs and (only is None or "runs" in only):
         make_runs(paths, [n for n in model_specs() if n != "bar_phasor"])
+    if only is None or "demos" in only:
+        make_demo_runs(args.reference, copy_demos(args.reference))
 
 
 if __name__ == "__main__":

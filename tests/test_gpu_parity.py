@@ -3,15 +3,16 @@ reference's per-sensor results for 16 seeds).  Random streams differ, so per-sen
 temperature and heat flux are compared over 16 seeds each side, in units of the combined
 standard error sqrt(SE_gpu^2 + SE_ref^2), SE = seed-to-seed standard deviation / sqrt(16).
 
-Pass criterion per model (T, flux x, flux y of every sensor): no |z| above 4.5 and at most
-5 % of the values (at least one allowed) above 3.  With independent z-scores the chance of a
-false failure is below 1 %."""
+Pass criterion per model (T, flux x, flux y of every sensor): no |z| above the bound of
+max_z (4.5, or Student's t at a 1 % family-wise rate where the values are many) and at most 5 %
+of the values (at least one allowed) above 3.  With independent z-scores the chance of a false
+failure is about 1 %."""
 import os
 
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, model_path
+from conftest import GOLDEN, demo_model_path, model_path
 
 pytestmark = pytest.mark.gpu
 
@@ -47,12 +48,23 @@ def zscores(a, b):
     return np.stack(zs, axis=1)
 
 
+def max_z(n: int) -> float:
+    """Largest |z| allowed among n values: Student's t (the combined SE comes from two 16-seed
+    spreads, about 30 degrees of freedom) at a 1 % family-wise rate over the n values, and never
+    below 4.5.  Up to about a thousand values that is the plain 4.5; the reference's larger demo
+    models compare 3000 and 9324 values, where a fixed 4.5 would fail on noise alone in about
+    one run out of six."""
+    from scipy.stats import t
+    return max(4.5, float(t.ppf(1.0 - 0.005 / n, 30)))
+
+
 def check(z, label):
     az = np.abs(z)
     over3 = int((az > 3.0).sum())
     allowed = max(1, int(0.05 * az.size))
-    print(f"{label}: max |z| {az.max():.2f}, {over3}/{az.size} above 3")
-    assert az.max() < 4.5, (label, az.max())
+    cap = max_z(az.size)
+    print(f"{label}: max |z| {az.max():.2f} (bound {cap:.2f}), {over3}/{az.size} above 3")
+    assert az.max() < cap, (label, az.max(), cap)
     assert over3 <= allowed, (label, over3)
 
 
@@ -61,6 +73,28 @@ def test_fp32_matches_reference(api, name):
     ref = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))["stats"]
     got = gpu_stats(api, name, api.FP32)
     check(zscores(got, ref), f"{name} fp32")
+
+
+@pytest.mark.parametrize("name", ["linear_demo", "linear_sides_demo_ss"])
+def test_fp32_matches_reference_on_its_demo_models(api, name, tmp_path):
+    """The reference's own demo models (psim_python/json/), against 16 seeded runs of the
+    reference built from its current sources.  The result tables the reference commits for
+    these models came from an older version of psim and lie several combined SE from its
+    current sources' runs; they are reported here, not used as the bar."""
+    gold = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))
+    ref = gold["stats"].astype(np.float64)
+    m = api.Model(demo_model_path(name, str(tmp_path)))
+    out = []
+    for seed in SEEDS:
+        m.run(seed=1000 + seed, precision=api.FP32)
+        out.append(m.measurements())
+    got = np.stack(out)
+    check(zscores(got, ref), f"{name} fp32")
+    committed = gold["committed"].astype(np.float64)
+    sd = ref[:, :, 0].std(axis=0, ddof=1)
+    z = (committed[:, 0] - ref[:, :, 0].mean(axis=0)) / np.where(sd > 0, sd, 1.0)
+    print(f"{name}: the reference's committed table against its current runs, mean z(T) {z.mean():.2f}, "
+          f"max |z(T)| {np.abs(z).max():.2f} (in seed-to-seed SD)")
 
 
 @pytest.mark.parametrize("name", ["bar_ss", "bar_full", "kinked_small", "plate_small"])
