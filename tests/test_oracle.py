@@ -80,6 +80,20 @@ def test_seeded_runs_match_reference(O, name, seeds):
             assert np.allclose(r.stats[:, 0], ref[:, 0], rtol=5e-3), (name, seed)
 
 
+def test_seeded_run_of_a_reference_demo_matches(O, tmp_path):
+    """The reference's own linear_demo model with the reference's seed 1: the oracle reproduces
+    its per-sensor results.  The demo fixtures keep float32, so the oracle's results are rounded
+    to float32 and must then be equal."""
+    from conftest import demo_model_path
+    gold = np.load(os.path.join(GOLDEN, "runs_linear_demo.npz"))
+    r = O.run(demo_model_path("linear_demo", str(tmp_path)), 1, threads=1)
+    ref = gold["stats"][list(gold["seeds"]).index(1)]
+    if os.uname().machine == "x86_64":
+        assert np.array_equal(r.stats.astype(np.float32), ref)
+    else:
+        assert np.allclose(r.stats[:, 0], ref[:, 0], rtol=5e-3)
+
+
 def test_multithreaded_oracle_is_the_same_process(O):
     """Several threads draw different streams but simulate the same process."""
     gold = np.load(os.path.join(GOLDEN, "runs_bar_ss.npz"))
