@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/psim_oracle.cpp).
 
 Test infrastructure only: the tests, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` use it as the checker.  The product never imports it.
+baseline leg of ``bench.py`` use it as the test oracle.  The product never imports it.
 """
 from __future__ import annotations
 

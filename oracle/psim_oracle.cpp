@@ -1,5 +1,5 @@
 // psim CPU oracle: a restatement of the reference psim Monte Carlo phonon
-// simulation, used ONLY as a test checker and as the timed CPU baseline.
+// simulation, used ONLY as a test oracle and as the timed CPU baseline.
 // Nothing in the product (psim_gb300/) links, imports or runs this file.
 //
 // It restates, in its own structure, the algorithms of the reference files

@@ -1,4 +1,4 @@
-"""CPU restatement of the surrogate network the GPU kernels compute (test checker).
+"""CPU restatement of the surrogate network the GPU kernels compute (a test oracle).
 
 Parameters per layer: W [in][out], b [out].  Hidden layers apply the exact GELU
 z Phi(z) = z (1 + erf(z / sqrt 2)) / 2, the output layer is linear, the loss is the mean squared

@@ -1,4 +1,4 @@
-"""CPU restatement of the steady-state criterion the GPU detector evaluates (test checker).
+"""CPU restatement of the steady-state criterion the GPU detector evaluates (a test oracle).
 
 Windows of W recorded steps per sensor over (energy count, flux x, flux y), flux in fixed point
 (2^20 units per m/s), each window split into B batches of W/B steps; a window's mean is the mean
