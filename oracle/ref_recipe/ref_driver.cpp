@@ -12,6 +12,7 @@
 //   tables <model.json> <dump.bin>                       material tables after initializeTables
 //   geom   <cases.txt> <out.txt>                         geometry known answers
 //   invert <model.json> <counts.txt> <out.txt>           E->T inversion of given counts
+//   topology <model.json> <out.txt>                      assembled cells and edge sub-surfaces
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -339,11 +340,50 @@ int cmdInvert(const std::string& model_path, const std::string& counts_path, con
     return 0;
 }
 
+// The assembled model: cells after Model::addCell's neighbour search (Cell::findTransitionSurface)
+// and the emitting surfaces after Model::setEmitSurface.  One line per cell, then one per
+// sub-surface of its edges in CompositeSurface order (transition surfaces, then emitting ones):
+//   c <sensor index> <x1> <y1> <x2> <y2> <x3> <y3> <spec of edge 0> <edge 1> <edge 2>
+//   t <cell> <edge> <neighbour cell> <x1> <y1> <x2> <y2>
+//   e <cell> <edge> <owning cell> <temp> <duration> <start time> <x1> <y1> <x2> <y2>
+// Cells and sensors are numbered by their position in the model (file order).
+int cmdTopology(const std::string& model_path, const std::string& out_path) {
+    const Value j = psim_json::parse_file(model_path);
+    auto model = buildModel(j);
+    const Cell* cells = model->cells_.data();
+    const Sensor* sensors = model->sensors_.data();
+    std::ofstream os(out_path);
+    os << std::setprecision(17);
+    auto put_line = [&os](const Line& l) { os << ' ' << l.p1.x << ' ' << l.p1.y << ' ' << l.p2.x << ' ' << l.p2.y; };
+    for (std::size_t c = 0; c < model->cells_.size(); ++c) {
+        const Cell& cell = model->cells_[c];
+        os << "c " << (&cell.sensor_ - sensors);
+        for (const Point& p : { cell.cell_.p1, cell.cell_.p2, cell.cell_.p3 }) { os << ' ' << p.x << ' ' << p.y; }
+        for (const auto& b : cell.boundaries_) { os << ' ' << b.main_surface_.getSpecularity(); }
+        os << '\n';
+        for (std::size_t e = 0; e < 3; ++e) {
+            const CompositeSurface& b = cell.boundaries_[e];
+            for (const auto& t : b.transition_sub_surfaces_) {
+                os << "t " << c << ' ' << e << ' ' << (&t.cell_ - cells);
+                put_line(t.getSurfaceLine());
+                os << '\n';
+            }
+            for (const auto& s : b.emit_sub_surfaces_) {
+                os << "e " << c << ' ' << e << ' ' << (&s.cell_ - cells) << ' ' << s.temp_ << ' ' << s.duration_ << ' '
+                   << s.start_time_;
+                put_line(s.getSurfaceLine());
+                os << '\n';
+            }
+        }
+    }
+    return 0;
+}
+
 }// namespace
 
 int main(int argc, char** argv) {
     if (argc < 2) {
-        std::cerr << "usage: ref_driver run|tables|geom|invert ...\n";
+        std::cerr << "usage: ref_driver run|tables|geom|invert|topology ...\n";
         return 2;
     }
     const std::string cmd = argv[1];
@@ -352,6 +392,7 @@ int main(int argc, char** argv) {
         if (cmd == "tables" && argc >= 4) { return cmdTables(argv[2], argv[3]); }
         if (cmd == "geom" && argc >= 4) { return cmdGeom(argv[2], argv[3]); }
         if (cmd == "invert" && argc >= 5) { return cmdInvert(argv[2], argv[3], argv[4]); }
+        if (cmd == "topology" && argc >= 4) { return cmdTopology(argv[2], argv[3]); }
     } catch (const std::exception& e) {
         std::cerr << "ref_driver error: " << e.what() << '\n';
         return 1;

@@ -10,6 +10,8 @@ Outputs (all small):
                          Triangle normals, area and getRandPoint on random and degenerate cases
   tables_<model>.npz     material tables after Model::initializeMaterialTables
   invert_<model>.npz     SensorInterpreter results for given tallies
+  topology_<model>.npz   the assembled model (cells, sensors, edge sub-surfaces) of every model
+                         file here, demos included
   runs_<model>.npz       per-sensor results of 16 seeded reference runs (statistical parity)
   models/<demo>.json.gz  the reference's own demo models (psim_python/json/), gzipped, and
   runs_<demo>.npz        16 seeded runs of each by the reference built from its sources, with
@@ -196,6 +198,42 @@ def make_tables(paths):
         print(f"tables_{name}.npz: {nt} temperatures, kept {keep}")
 
 
+# ---------------------------------------------------------------- model assembly
+def read_topology(path):
+    """The reference's assembled model as written by `ref_driver topology`: per cell its sensor,
+    vertices and edge specularities; per edge sub-surface its cell, edge, kind (0 transition,
+    1 emitting), target (neighbour cell, or the emitting surface's owning cell), line and, for
+    emitting surfaces, (temperature, duration, start time)."""
+    cells, subs = [], []
+    for line in open(path):
+        f = line.split()
+        if f[0] == "c":
+            cells.append([float(v) for v in f[1:]])
+        elif f[0] == "t":
+            subs.append([int(f[1]), int(f[2]), 0, int(f[3])] + [float(v) for v in f[4:8]] + [np.nan] * 3)
+        elif f[0] == "e":
+            vals = [float(v) for v in f[4:]]
+            subs.append([int(f[1]), int(f[2]), 1, int(f[3])] + vals[3:7] + vals[0:3])
+    c = np.array(cells, dtype=np.float64)
+    s = np.array(subs, dtype=np.float64).reshape(-1, 11)
+    return dict(cell_sensor=c[:, 0].astype(np.int64), cell_vertices=c[:, 1:7], cell_spec=c[:, 7:10],
+                sub_cell=s[:, 0].astype(np.int64), sub_edge=s[:, 1].astype(np.int64), sub_kind=s[:, 2].astype(np.int64),
+                sub_target=s[:, 3].astype(np.int64), sub_line=s[:, 4:8], sub_emit=s[:, 8:11])
+
+
+def make_topology(paths):
+    """topology_<model>.npz: the reference's model assembly (Model::addCell's neighbour search,
+    Model::setEmitSurface) for every model file the fixtures use."""
+    for name, path in paths.items():
+        with tempfile.TemporaryDirectory() as td:
+            out = os.path.join(td, "t.txt")
+            driver("topology", path, out)
+            topo = read_topology(out)
+        np.savez_compressed(os.path.join(HERE, f"topology_{name}.npz"), **topo)
+        print(f"topology_{name}.npz: {len(topo['cell_sensor'])} cells, {int((topo['sub_kind'] == 0).sum())} transition "
+              f"and {int((topo['sub_kind'] == 1).sum())} emitting sub-surfaces")
+
+
 # ---------------------------------------------------------------- inversion
 def make_invert(paths):
     rng = np.random.default_rng(7)
@@ -305,8 +343,11 @@ def main():
         make_invert(paths)
     if not args.skip_runs and (only is None or "runs" in only):
         make_runs(paths, [n for n in model_specs() if n != "bar_phasor"])
+    demo_paths = copy_demos(args.reference) if only is None or "demos" in only or "topology" in only else {}
+    if only is None or "topology" in only:
+        make_topology({**paths, **demo_paths})
     if only is None or "demos" in only:
-        make_demo_runs(args.reference, copy_demos(args.reference))
+        make_demo_runs(args.reference, demo_paths)
 
 
 if __name__ == "__main__":
