@@ -121,23 +121,30 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.f.close()
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.out_path):
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
-            except ValueError:
-                continue
-            for name, flag in zip(names, parts[5:9]):
-                if flag.lower() == "active":
-                    reasons.add(name)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+        return parse_clocks(open(self.out_path).read().splitlines(), gpu_index)
+
+
+def parse_clocks(lines, gpu_index: int = 0) -> dict:
+    """Median SM clock, maximum clock and the throttle reasons seen, from nvidia-smi samples
+    (index, clocks.sm, clocks.max.sm, power.draw, active reasons, hw_slowdown,
+    hw_thermal_slowdown, sw_thermal_slowdown, sw_power_cap) of one GPU."""
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in lines:
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
+            continue
+        try:
+            sm.append(float(parts[1]))
+            mx.append(float(parts[2]))
+        except ValueError:
+            continue
+        for name, flag in zip(names, parts[5:9]):
+            if flag.lower() == "active":
+                reasons.add(name)
+    if not sm:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def cpu_sample(path_dir: str, budget: int, threads: int, seed: int, steps: int = STEPS, dt_ps: float = DT_PS):

@@ -1,0 +1,58 @@
+"""bench.py without a GPU: the reference arm's JSON line (the CPU oracle on host threads, on a
+bounded sample of the kinked workload), its silence on ranks other than 0, and the parsing of
+the nvidia-smi clock samples that decide whether a timed run throttled."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+sys.path.insert(0, ROOT)
+import bench  # noqa: E402
+
+
+def run_bench(args, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                          env=e, timeout=600)
+
+
+def test_reference_arm_prints_one_contract_line(built):
+    out = run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0", "--measurements", "200",
+                     "--cpu-budget", "20000"])
+    assert out.returncode == 0, out.stderr
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["metric"] == "phonon-steps/s" and d["unit"] == "phonon-steps/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 0
+    assert "kinked" in d["config"]["workload"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_is_silent_on_other_ranks():
+    out = run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0"], env={"RANK": "1", "WORLD_SIZE": "2"})
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == ""
+
+
+def test_clock_samples_report_median_and_throttle_reasons():
+    rows = [
+        "0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1965, 2070, 1395.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1200.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "1, 800, 2070, 300.0, 0x0000000000000008, Active, Not Active, Not Active, Not Active",  # another GPU
+        "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active",  # unreadable sample
+    ]
+    c = bench.parse_clocks(rows, 0)
+    assert c == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    c1 = bench.parse_clocks(rows, 1)
+    assert c1["reasons"] == ["hw_slowdown"] and c1["sm_mhz"] == 800.0
+    assert bench.parse_clocks([], 0)["reasons"] == ["no samples"]
