@@ -66,6 +66,64 @@ template<typename T> std::vector<T> copy_of(const T* p, std::size_t n, const cha
     return n > 0 ? std::vector<T>(p, p + n) : std::vector<T>{};
 }
 
+// The ABI views of the flattened model and of its interpreter description: pointers into d.
+void fill_sim_desc(const psim::gpu::SimDesc& d, psim_sim_desc* out) {
+    *out = psim_sim_desc{};
+    out->measurement_steps = d.steps;
+    out->simulation_time = d.sim_time;
+    out->phasor_sim = d.phasor ? 1 : 0;
+    out->sim_type = d.sim_type;
+    out->step_adjustment = d.step_adj;
+    out->recorded_steps = d.recorded;
+    out->full_simulation = d.full ? 1 : 0;
+    out->n_materials = d.n_materials;
+    out->mat_freq = d.mat_freq.data();
+    out->mat_vel = d.mat_vel.data();
+    out->mat_params = d.mat_params.data();
+    out->n_tables = d.n_tables;
+    out->tables = d.tables.data();
+    out->n_sensors = d.n_sensors;
+    out->sensor_material = d.sensor_material.data();
+    out->sensor_temp = d.sensor_temp.data();
+    out->sensor_base_table = d.sensor_base_table.data();
+    out->sensor_scatter_table = d.sensor_scatter_table.data();
+    out->n_cells = d.n_cells;
+    out->cell_vertices = d.cell_vertices.data();
+    out->cell_sensor = d.cell_sensor.data();
+    out->cell_spec = d.cell_spec.data();
+    out->edge_sub_begin = d.edge_sub_begin.data();
+    out->n_subs = static_cast<uint32_t>(d.sub_kind.size());
+    out->sub_kind = d.sub_kind.data();
+    out->sub_target = d.sub_target.data();
+    out->sub_line = d.sub_line.data();
+    out->n_emitters = d.n_emitters;
+    out->emit_cell = d.emit_cell.data();
+    out->emit_edge = d.emit_edge.data();
+    out->emit_line = d.emit_line.data();
+    out->emit_temp = d.emit_temp.data();
+    out->emit_start = d.emit_start.data();
+    out->emit_duration = d.emit_duration.data();
+    out->emit_table = d.emit_table.data();
+}
+
+void fill_interp_desc(const psim::gpu::InterpDesc& d, psim_interp_desc* out) {
+    *out = psim_interp_desc{};
+    out->n_sensors = d.n_sensors;
+    out->recorded_steps = d.recorded;
+    out->t_eq = d.t_eq;
+    out->eff_energy = d.eff_energy;
+    out->lower_bound = d.lb;
+    out->upper_bound = d.ub;
+    out->sensor_area = d.area.data();
+    out->sensor_heat_capacity = d.heat_capacity.data();
+    out->sensor_init_temp = d.init_temp.data();
+    out->sensor_material = d.material.data();
+    out->n_materials = static_cast<uint32_t>(d.mat_temp_begin.size() - 1);
+    out->mat_temp_begin = d.mat_temp_begin.data();
+    out->temps = d.temps.data();
+    out->energies = d.energies.data();
+}
+
 }// namespace
 
 extern "C" {
@@ -112,9 +170,10 @@ int psim_model_shape(const psim_model* m, int64_t* n_sensors, int64_t* n_recorde
 int psim_model_measurements(const psim_model* m, double* stats) {
     if (m == nullptr || stats == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     if (m->m->measurements().empty()) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
-    const auto a = m->m->averaged();
-    for (std::size_t i = 0; i < a.size(); ++i) { std::memcpy(stats + 6 * i, a[i].data(), 6 * sizeof(double)); }
-    return PSIM_OK;
+    return guard([&]() {
+        const auto a = m->m->averaged();
+        for (std::size_t i = 0; i < a.size(); ++i) { std::memcpy(stats + 6 * i, a[i].data(), 6 * sizeof(double)); }
+    });
 }
 
 int psim_model_series(const psim_model* m, int64_t run, double* temps, double* fluxes) {
@@ -162,9 +221,10 @@ int psim_model_population(const psim_model* m, uint32_t* out) {
 
 int psim_model_start_temps(const psim_model* m, double* out) {
     if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
-    const auto t = m->m->start_temps();
-    std::copy(t.begin(), t.end(), out);
-    return PSIM_OK;
+    return guard([&]() {
+        const auto t = m->m->start_temps();
+        std::copy(t.begin(), t.end(), out);
+    });
 }
 
 int psim_model_set_start_temps(psim_model* m, const double* temps) {
@@ -182,67 +242,16 @@ int psim_model_export(const psim_model* m, const char* json_path, double seconds
 
 int psim_model_sim_desc(const psim_model* m, psim_sim_desc* out) {
     if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
-    const psim::gpu::SimDesc& d = m->m->sim_desc();
-    *out = psim_sim_desc{};
-    out->measurement_steps = d.steps;
-    out->simulation_time = d.sim_time;
-    out->phasor_sim = d.phasor ? 1 : 0;
-    out->sim_type = d.sim_type;
-    out->step_adjustment = d.step_adj;
-    out->recorded_steps = d.recorded;
-    out->full_simulation = d.full ? 1 : 0;
-    out->n_materials = d.n_materials;
-    out->mat_freq = d.mat_freq.data();
-    out->mat_vel = d.mat_vel.data();
-    out->mat_params = d.mat_params.data();
-    out->n_tables = d.n_tables;
-    out->tables = d.tables.data();
-    out->n_sensors = d.n_sensors;
-    out->sensor_material = d.sensor_material.data();
-    out->sensor_temp = d.sensor_temp.data();
-    out->sensor_base_table = d.sensor_base_table.data();
-    out->sensor_scatter_table = d.sensor_scatter_table.data();
-    out->n_cells = d.n_cells;
-    out->cell_vertices = d.cell_vertices.data();
-    out->cell_sensor = d.cell_sensor.data();
-    out->cell_spec = d.cell_spec.data();
-    out->edge_sub_begin = d.edge_sub_begin.data();
-    out->n_subs = static_cast<uint32_t>(d.sub_kind.size());
-    out->sub_kind = d.sub_kind.data();
-    out->sub_target = d.sub_target.data();
-    out->sub_line = d.sub_line.data();
-    out->n_emitters = d.n_emitters;
-    out->emit_cell = d.emit_cell.data();
-    out->emit_edge = d.emit_edge.data();
-    out->emit_line = d.emit_line.data();
-    out->emit_temp = d.emit_temp.data();
-    out->emit_start = d.emit_start.data();
-    out->emit_duration = d.emit_duration.data();
-    out->emit_table = d.emit_table.data();
-    return PSIM_OK;
+    return guard([&]() { fill_sim_desc(m->m->sim_desc(), out); });
 }
 
 int psim_model_interp_desc(const psim_model* m, double eff_energy, psim_interp_desc* out) {
     if (m == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     auto* mm = const_cast<psim_model*>(m);
-    mm->interp_cache = m->m->interp_for(eff_energy);
-    const psim::gpu::InterpDesc& d = mm->interp_cache;
-    *out = psim_interp_desc{};
-    out->n_sensors = d.n_sensors;
-    out->recorded_steps = d.recorded;
-    out->t_eq = d.t_eq;
-    out->eff_energy = d.eff_energy;
-    out->lower_bound = d.lb;
-    out->upper_bound = d.ub;
-    out->sensor_area = d.area.data();
-    out->sensor_heat_capacity = d.heat_capacity.data();
-    out->sensor_init_temp = d.init_temp.data();
-    out->sensor_material = d.material.data();
-    out->n_materials = static_cast<uint32_t>(d.mat_temp_begin.size() - 1);
-    out->mat_temp_begin = d.mat_temp_begin.data();
-    out->temps = d.temps.data();
-    out->energies = d.energies.data();
-    return PSIM_OK;
+    return guard([&]() {
+        mm->interp_cache = m->m->interp_for(eff_energy);
+        fill_interp_desc(mm->interp_cache, out);
+    });
 }
 
 void psim_model_destroy(psim_model* m) { delete m; }
