@@ -1,6 +1,7 @@
 // psim_gb300 command line: the drop-in for `psim a.json [b.json ...]` (psim/src/main.cpp:10-31).
 // Each model file is read, run on the GPU and written to ss_<name>.txt or per_<name>.txt next
-// to it.  Options (before the files): --seed N, --fp64.
+// to it.  Options (before the files): --seed N, --fp64.  The messages are the reference's; the
+// exit status is 1 when any file could not be read, run or written (the reference exits 0).
 #include <chrono>
 #include <cstdint>
 #include <cstdio>
@@ -25,7 +26,7 @@ int main(int argc, char** argv) {
         }
     }
     if (files.empty()) {
-        std::printf("Need filenames\n");
+        std::printf("Need filenames\ndone\n");
         return 0;
     }
     int status = 0;

@@ -254,3 +254,21 @@ def test_start_temperatures_are_checked_and_reset(api):
     with pytest.raises(api.PsimError) as e:
         full.set_start_temps(np.full(full.n_sensors, 50.0))
     assert e.value.code == api.PSIM_ERR_INVALID
+
+
+def test_command_line_messages(api, tmp_path):
+    """The psim_gb300 command line prints the reference's messages (psim/src/main.cpp:10-31)
+    and reports a failed file through its exit status."""
+    import subprocess
+    from psim_gb300 import build
+    cli = build.CLI
+    out = subprocess.run([cli], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout == "Need filenames\ndone\n"
+    missing = str(tmp_path / "missing.json")
+    out = subprocess.run([cli, missing], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and out.stdout.endswith("done\n")
+    assert f'There was an error reading the data from the file at "{missing}"' in out.stderr
+    if api.device_count() == 0:  # no device: the run fails loudly, nothing is written
+        out = subprocess.run([cli, model_path("bar_ss")], capture_output=True, text=True, timeout=60)
+        assert out.returncode == 1 and "run failed" in out.stderr and "CUDA" in out.stderr
+        assert not os.path.exists(os.path.join(os.path.dirname(model_path("bar_ss")), "ss_bar_ss.txt"))
