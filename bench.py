@@ -209,6 +209,24 @@ def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
     return out
 
 
+def precision_error(s32: np.ndarray, s64: np.ndarray) -> dict:
+    """Error of FP32 runs against FP64 runs of the same random streams.  s32, s64: per-seed
+    measurement tables [seeds, sensors, 6] (T, SE, flux x, SE, flux y, SE).  Temperature keeps
+    its historical keys; each quantity also gets its differences against the FP64 runs'
+    seed-to-seed spread."""
+    out = {"quantity": "per-sensor mean temperature over the run"}
+    for name, col, unit in (("T", 0, "K"), ("flux_x", 2, "psim flux column"), ("flux_y", 4, "psim flux column")):
+        diff = np.abs(s32[:, :, col] - s64[:, :, col])
+        noise = float(s64[:, :, col].std(axis=0, ddof=1).mean())
+        row = {"mean_abs_diff": float(diff.mean()), "max_abs_diff": float(diff.max()), "seed_to_seed_sd": noise,
+               "mean_diff_over_sd": float(diff.mean() / noise) if noise > 0 else None, "unit": unit}
+        if name == "T":
+            out.update({"mean_abs_diff_K": row["mean_abs_diff"], "max_abs_diff_K": row["max_abs_diff"],
+                        "seed_to_seed_sd_K": noise, "mean_diff_over_sd": row["mean_diff_over_sd"]})
+        out[name] = row
+    return out
+
+
 def workload_name(args) -> str:
     return (f"kinked 3-arm structure, 400 quadrilateral cells / sensors, periodic, dt {args.dt_ps:g} ps, "
             f"{args.measurements} steps, output every 50 steps, {args.per_step:.0e} phonons per step")
@@ -388,17 +406,12 @@ def main():
         per_step = 2.0e4
         small = api.Model(model_json(os.path.join(td, "kinked_fp64.json"), int(per_step * steps_n / lifetime), steps_n,
                                      args.dt_ps))
-        t32, t64 = [], []
+        s32, s64 = [], []
         for seed in range(1, 5):
-            t32.append(small.run(seed=seed, precision=api.FP32).measurements()[:, 0])
-            t64.append(small.run(seed=seed, precision=api.FP64).measurements()[:, 0])
-        t32, t64 = np.array(t32), np.array(t64)
-        diff = np.abs(t32 - t64)
-        noise = t64.std(axis=0, ddof=1).mean()
-        fp64_check = {"workload": f"the same model at {per_step:.0e} phonons per step, 4 seeds, FP32 and FP64 kernels on the same random streams",
-                      "quantity": "per-sensor mean temperature over the run",
-                      "mean_abs_diff_K": float(diff.mean()), "max_abs_diff_K": float(diff.max()),
-                      "seed_to_seed_sd_K": float(noise), "mean_diff_over_sd": float(diff.mean() / noise)}
+            s32.append(small.run(seed=seed, precision=api.FP32).measurements())
+            s64.append(small.run(seed=seed, precision=api.FP64).measurements())
+        fp64_check = {"workload": f"the same model at {per_step:.0e} phonons per step, 4 seeds, FP32 and FP64 kernels on the same random streams"}
+        fp64_check.update(precision_error(np.array(s32), np.array(s64)))
 
     # the batched workload: independent random rectangles (uneven cells and populations) run
     # concurrently, options from the autotuner, in chunks of BATCH_CHUNK models alive at once

@@ -1,10 +1,13 @@
 """bench.py without a GPU: the reference arm's JSON line (the CPU oracle on host threads, on a
-bounded sample of the kinked workload), its silence on ranks other than 0, and the parsing of
-the nvidia-smi clock samples that decide whether a timed run throttled."""
+bounded sample of the kinked workload), its silence on ranks other than 0, the parsing of the
+nvidia-smi clock samples that decide whether a timed run throttled, and the summary of the FP32
+kernel's error against FP64 runs of the same random streams."""
 import json
 import os
 import subprocess
 import sys
+
+import numpy as np
 
 from conftest import ROOT
 
@@ -56,3 +59,20 @@ def test_clock_samples_report_median_and_throttle_reasons():
     c1 = bench.parse_clocks(rows, 1)
     assert c1["reasons"] == ["hw_slowdown"] and c1["sm_mhz"] == 800.0
     assert bench.parse_clocks([], 0)["reasons"] == ["no samples"]
+
+
+def test_precision_error_covers_temperature_and_flux():
+    rng = np.random.default_rng(0)
+    s64 = rng.normal(300.0, 0.05, size=(4, 10, 6))
+    s64[:, :, 2] = rng.normal(5e3, 40.0, size=(4, 10))
+    s64[:, :, 4] = rng.normal(0.0, 40.0, size=(4, 10))
+    s32 = s64.copy()
+    s32[:, :, 0] += 0.01
+    s32[1, 3, 2] += 8.0
+    e = bench.precision_error(s32, s64)
+    assert np.isclose(e["T"]["mean_abs_diff"], 0.01) and np.isclose(e["mean_abs_diff_K"], 0.01)
+    assert np.isclose(e["max_abs_diff_K"], 0.01) and e["seed_to_seed_sd_K"] == e["T"]["seed_to_seed_sd"]
+    assert np.isclose(e["flux_x"]["max_abs_diff"], 8.0) and np.isclose(e["flux_x"]["mean_abs_diff"], 8.0 / 40)
+    assert e["flux_y"]["max_abs_diff"] == 0.0 and e["flux_y"]["mean_diff_over_sd"] == 0.0
+    sd = s64[:, :, 2].std(axis=0, ddof=1).mean()
+    assert np.isclose(e["flux_x"]["mean_diff_over_sd"], (8.0 / 40) / sd)
