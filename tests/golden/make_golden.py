@@ -16,6 +16,7 @@ Outputs (all small):
   models/<demo>.json.gz  the reference's own demo models (psim_python/json/), gzipped, and
   runs_<demo>.npz        16 seeded runs of each by the reference built from its sources, with
                          the result table the reference commits for it (psim_python/json/results/)
+  seeded_<demo>.npz      one seeded run of the largest demo at a reduced phonon budget
 """
 from __future__ import annotations
 
@@ -309,10 +310,10 @@ def copy_demos(reference):
     return paths
 
 
-def make_demo_runs(reference, paths):
+def make_demo_runs(reference, paths, names=DEMOS):
     """16 seeded reference runs of each demo, next to the steady-state table the reference
     commits for it (a single unseeded run: T, SE, flux x, SE, flux y, SE per sensor)."""
-    for name in DEMOS:
+    for name in names:
         committed = np.loadtxt(os.path.join(reference, "psim_python", "json", "results", f"ss_{name}.txt"), skiprows=1)
         with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
             res = list(pool.map(lambda s: ref_run(paths[name], s), SEEDS))
@@ -324,11 +325,36 @@ def make_demo_runs(reference, paths):
         print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}, committed {committed[:4, 0]}")
 
 
+SEEDED_DEMO = ("kinked_demo_120_35_spec", 20000, 1)  # demo, reduced phonon budget, seed
+
+
+def reduced_budget(src, dst, num_phonons):
+    """The model file src with its phonon budget set to num_phonons (everything else as is)."""
+    d = json.load(open(src))
+    d["settings"]["num_phonons"] = num_phonons
+    with open(dst, "w") as f:
+        json.dump(d, f)
+    return dst
+
+
+def make_demo_seeded(paths):
+    """seeded_<demo>.npz: one seeded reference run of the largest demo at a reduced phonon
+    budget, in full precision, for a bit-exact check of the oracle on that geometry."""
+    name, budget, seed = SEEDED_DEMO
+    with tempfile.TemporaryDirectory() as td:
+        p = reduced_budget(paths[name], os.path.join(td, name + ".json"), budget)
+        stats, phonons = ref_run(p, seed)
+    np.savez_compressed(os.path.join(HERE, f"seeded_{name}.npz"), seed=seed, num_phonons=budget, stats=stats,
+                        phonons=phonons)
+    print(f"seeded_{name}.npz: budget {budget}, seed {seed}, {phonons} phonons")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-runs", action="store_true")
     ap.add_argument("--only", default="")
+    ap.add_argument("--demo", default="", help="comma-separated demo models for the demo runs (default: all three)")
     args = ap.parse_args()
     if not O.build_reference(args.reference):
         sys.exit("the reference sources are not available")
@@ -343,11 +369,13 @@ def main():
         make_invert(paths)
     if not args.skip_runs and (only is None or "runs" in only):
         make_runs(paths, [n for n in model_specs() if n != "bar_phasor"])
-    demo_paths = copy_demos(args.reference) if only is None or "demos" in only or "topology" in only else {}
+    demo_paths = copy_demos(args.reference) if only is None or {"demos", "topology", "seeded"} & only else {}
+    if only is None or "seeded" in only:
+        make_demo_seeded(demo_paths)
     if only is None or "topology" in only:
         make_topology({**paths, **demo_paths})
     if only is None or "demos" in only:
-        make_demo_runs(args.reference, demo_paths)
+        make_demo_runs(args.reference, demo_paths, args.demo.split(",") if args.demo else DEMOS)
 
 
 if __name__ == "__main__":

@@ -94,6 +94,25 @@ def test_seeded_run_of_a_reference_demo_matches(O, tmp_path):
         assert np.allclose(r.stats[:, 0], ref[:, 0], rtol=5e-3)
 
 
+def test_seeded_run_of_the_largest_reference_demo_matches(O, tmp_path):
+    """The reference's kinked demo (6174 cells, 3108 sensors, 42 emitting surfaces) at a reduced
+    phonon budget with the reference's seed: the oracle reproduces its per-sensor results."""
+    import json
+    from conftest import demo_model_path
+    gold = np.load(os.path.join(GOLDEN, "seeded_kinked_demo_120_35_spec.npz"))
+    d = json.load(open(demo_model_path("kinked_demo_120_35_spec", str(tmp_path))))
+    d["settings"]["num_phonons"] = int(gold["num_phonons"])
+    path = str(tmp_path / "kinked_demo_reduced.json")
+    with open(path, "w") as f:
+        json.dump(d, f)
+    r = O.run(path, int(gold["seed"]), threads=1)
+    assert r.stats.shape == gold["stats"].shape == (3108, 6)
+    if os.uname().machine == "x86_64":
+        assert np.array_equal(r.stats, gold["stats"])
+    else:
+        assert np.allclose(r.stats[:, 0], gold["stats"][:, 0], rtol=5e-3)
+
+
 def test_multithreaded_oracle_is_the_same_process(O):
     """Several threads draw different streams but simulate the same process."""
     gold = np.load(os.path.join(GOLDEN, "runs_bar_ss.npz"))
