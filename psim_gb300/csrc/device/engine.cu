@@ -282,14 +282,46 @@ int device_count() noexcept {
     return n;
 }
 
+namespace {
+
+// The inputs of the scattering rates (Material::relaxRates, psim/src/material.cpp:54-62).  The
+// kernels' event loops end only when every rate is finite and non-negative: a negative or NaN
+// rate sum gives a negative or NaN time to the next scattering event, and the step boundary is
+// then never reached.  So the relaxation coefficients must be finite and non-negative and the
+// sensor temperatures positive and finite; both are checked before any device work.
+void check_rate_inputs(const SimDesc& d) {
+    if (d.mat_params.size() < static_cast<std::size_t>(d.n_materials) * 8 || d.sensor_temp.size() < d.n_sensors) {
+        throw std::invalid_argument("missing material parameters or sensor temperatures");
+    }
+    for (std::uint32_t m = 0; m < d.n_materials; ++m) {
+        const double* pr = &d.mat_params[8 * static_cast<std::size_t>(m)];
+        for (int k = 0; k < 4; ++k) {// b_l, b_tn, b_tu, b_i
+            if (!std::isfinite(pr[k]) || pr[k] < 0.) {
+                throw std::invalid_argument("relaxation coefficients must be finite and non-negative (material "
+                                            + std::to_string(m) + ")");
+            }
+        }
+        if (!std::isfinite(pr[4])) { throw std::invalid_argument("the relaxation cut-off frequency w must be finite"); }
+    }
+    for (std::uint32_t s = 0; s < d.n_sensors; ++s) {
+        const double T = d.sensor_temp[s];
+        if (!(T > 0.) || !std::isfinite(T)) {
+            throw std::invalid_argument("sensor temperatures must be positive and finite (sensor " + std::to_string(s) + ")");
+        }
+    }
+}
+
+}// namespace
+
 Engine::Engine(const SimDesc& d)
     : desc_{ d }
     , impl_{ std::make_unique<Impl>() } {
-    if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
     if (d.n_cells == 0 || d.n_sensors == 0 || d.n_materials == 0 || d.steps == 0) { throw std::invalid_argument("empty model"); }
     if (d.n_materials > kMaxMaterials) { throw std::invalid_argument("at most 16 materials are supported"); }
     if (d.n_cells >= (1U << 24)) { throw std::invalid_argument("at most 2^24 - 1 cells are supported"); }
     if (d.steps >= 0xFFFFFFFFULL) { throw std::invalid_argument("too many measurement steps"); }
+    check_rate_inputs(d);
+    if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
     Impl& I = *impl_;
     int dev = 0;
     check(cudaGetDevice(&dev), "cudaGetDevice");

@@ -137,6 +137,10 @@ void HostModel::set_type(SimType t, std::size_t interval) {// Model::setSimulati
 }
 
 void HostModel::add_sensor(std::uint64_t id, std::uint32_t material, double t_init) {// model.cpp:81-96
+    // the scattering rates take the sensor's temperature: it must be a temperature
+    if (!(t_init > 0.) || !std::isfinite(t_init)) {
+        throw std::runtime_error("Sensor temperature must be positive and finite: sensor " + std::to_string(id));
+    }
     for (const auto& s : sensors_) {
         if (s.id == id) { throw std::runtime_error("Sensor with this ID already exists"); }
     }
@@ -299,6 +303,13 @@ std::unique_ptr<HostModel> HostModel::from_json(const std::string& path) {// Inp
         sp.b_tu = r.at("b_tu").as_double();
         sp.b_i = r.at("b_i").as_double();
         sp.w = r.at("w").as_double();
+        // the rates must stay finite and non-negative for every event loop to end
+        for (const double b : { sp.b_l, sp.b_tn, sp.b_tu, sp.b_i }) {
+            if (!std::isfinite(b) || b < 0.) {
+                throw std::runtime_error("Relaxation coefficients must be finite and non-negative: " + sp.name);
+            }
+        }
+        if (!std::isfinite(sp.w)) { throw std::runtime_error("Relaxation cut-off frequency must be finite: " + sp.name); }
         by_name[sp.name] = static_cast<std::uint32_t>(m->mat_specs_.size());
         m->mat_specs_.push_back(sp);
         m->mats_.emplace_back(sp, m->t_eq_ == 0.);

@@ -272,3 +272,43 @@ def test_command_line_messages(api, tmp_path):
         out = subprocess.run([cli, model_path("bar_ss")], capture_output=True, text=True, timeout=60)
         assert out.returncode == 1 and "run failed" in out.stderr and "CUDA" in out.stderr
         assert not os.path.exists(os.path.join(os.path.dirname(model_path("bar_ss")), "ss_bar_ss.txt"))
+
+
+def test_rate_inputs_are_refused_before_any_device_work(api, tmp_path):
+    """A negative relaxation coefficient or a non-positive sensor temperature would make a
+    scattering rate negative; the kernels' event loops cannot end a step with a negative
+    scattering time, so such inputs are refused on the host, at load and at the simulator seam."""
+    import ctypes
+    from psim_gb300 import modelgen as mg
+    base = mg.bar(num_cells=3, num_phonons=1000, num_measurements=100, sim_time=1.0)
+    m = json.loads(json.dumps(base))
+    m["materials"][0]["r_data"]["b_i"] = -1.2e-45
+    with pytest.raises(api.PsimError, match="Relaxation coefficients") as e:
+        api.Model(_write(str(tmp_path), m))
+    assert e.value.code == api.PSIM_ERR_INVALID
+    for t in (0.0, -5.0):
+        m = json.loads(json.dumps(base))
+        m["sensors"][1]["t_init"] = t
+        with pytest.raises(api.PsimError, match="Sensor temperature"):
+            api.Model(_write(str(tmp_path), m))
+    # the simulator seam takes the rate temperatures and coefficients from its caller
+    model = api.Model(model_path("bar_ss"))
+    d = model.sim_desc()
+    temps = np.ctypeslib.as_array(d.sensor_temp, shape=(d.n_sensors,)).copy()
+    params = np.ctypeslib.as_array(d.mat_params, shape=(8 * d.n_materials,)).copy()
+    for bad in (0.0, -300.0, np.nan, np.inf):
+        t = temps.copy()
+        t[3] = bad
+        d.sensor_temp = t.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        with pytest.raises(api.PsimError, match="sensor temperatures") as e:
+            api.Simulator(d)
+        assert e.value.code == api.PSIM_ERR_INVALID
+    d.sensor_temp = temps.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    for k, bad in ((0, -2e-24), (3, np.nan), (2, np.inf)):
+        p = params.copy()
+        p[k] = bad
+        d.mat_params = p.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        with pytest.raises(api.PsimError, match="relaxation coefficients") as e:
+            api.Simulator(d)
+        assert e.value.code == api.PSIM_ERR_INVALID
+    model.close()
