@@ -311,6 +311,22 @@ void check_rate_inputs(const SimDesc& d) {
     }
 }
 
+// The run's time line: a positive simulated time, and emitting windows inside it
+// (Model::setEmitSurface's rule, psim/src/model.cpp:125-133), so that birth steps are in range.
+void check_time_line(const SimDesc& d) {
+    if (!(d.sim_time > 0.) || !std::isfinite(d.sim_time)) { throw std::invalid_argument("simulation time must be positive and finite"); }
+    if (d.emit_start.size() < d.n_emitters || d.emit_duration.size() < d.n_emitters) {
+        throw std::invalid_argument("missing emitter start times or durations");
+    }
+    for (std::uint32_t e = 0; e < d.n_emitters; ++e) {
+        const double start = d.emit_start[e];
+        const double dur = d.emit_duration[e];
+        if (!(start >= 0.) || !(start < d.sim_time) || !(dur >= 0.) || !(dur <= d.sim_time - start)) {
+            throw std::invalid_argument("emitter start time or duration outside the simulated time (emitter " + std::to_string(e) + ")");
+        }
+    }
+}
+
 }// namespace
 
 Engine::Engine(const SimDesc& d)
@@ -321,6 +337,7 @@ Engine::Engine(const SimDesc& d)
     if (d.n_cells >= (1U << 24)) { throw std::invalid_argument("at most 2^24 - 1 cells are supported"); }
     if (d.steps >= 0xFFFFFFFFULL) { throw std::invalid_argument("too many measurement steps"); }
     check_rate_inputs(d);
+    check_time_line(d);
     if (device_count() <= 0) { throw std::runtime_error("no CUDA device is available"); }
     Impl& I = *impl_;
     int dev = 0;
@@ -474,6 +491,7 @@ std::uint64_t Engine::init_builders(double t_eq, double eff_energy, const double
         if (!(energy > 0.) || !(eff_energy > 0.)) { return 0; }
         double whole = 0.;
         const double frac = std::modf(energy / eff_energy, &whole);
+        if (!(whole < 4294967295.)) { throw std::length_error("more than 2^32 - 1 phonons in one run"); }
         auto n = static_cast<std::uint64_t>(whole);
         return (uni(rng) < frac) ? n + 1 : n;
     };

@@ -277,7 +277,8 @@ def test_command_line_messages(api, tmp_path):
 def test_rate_inputs_are_refused_before_any_device_work(api, tmp_path):
     """A negative relaxation coefficient or a non-positive sensor temperature would make a
     scattering rate negative; the kernels' event loops cannot end a step with a negative
-    scattering time, so such inputs are refused on the host, at load and at the simulator seam."""
+    scattering time, so such inputs are refused on the host, at load and at the simulator seam.
+    The seam also refuses a non-positive simulated time and emitting windows outside it."""
     import ctypes
     from psim_gb300 import modelgen as mg
     base = mg.bar(num_cells=3, num_phonons=1000, num_measurements=100, sim_time=1.0)
@@ -309,6 +310,24 @@ def test_rate_inputs_are_refused_before_any_device_work(api, tmp_path):
         p[k] = bad
         d.mat_params = p.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         with pytest.raises(api.PsimError, match="relaxation coefficients") as e:
+            api.Simulator(d)
+        assert e.value.code == api.PSIM_ERR_INVALID
+    d.mat_params = params.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    # and the time line: a positive simulated time, emitting windows inside it
+    sim_time = d.simulation_time
+    for bad in (0.0, -1.0, np.nan):
+        d.simulation_time = bad
+        with pytest.raises(api.PsimError, match="simulation.time"):
+            api.Simulator(d)
+    d.simulation_time = sim_time
+    start = np.ctypeslib.as_array(d.emit_start, shape=(d.n_emitters,)).copy()
+    dur = np.ctypeslib.as_array(d.emit_duration, shape=(d.n_emitters,)).copy()
+    for s0, du in ((-0.1, 0.5), (sim_time, 0.0), (0.0, sim_time * 1.01), (0.5 * sim_time, 0.6 * sim_time), (0.0, -1.0)):
+        s1, d1 = start.copy(), dur.copy()
+        s1[1], d1[1] = s0, du
+        d.emit_start = s1.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.emit_duration = d1.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        with pytest.raises(api.PsimError, match="emitter start time or duration") as e:
             api.Simulator(d)
         assert e.value.code == api.PSIM_ERR_INVALID
     model.close()
