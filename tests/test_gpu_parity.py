@@ -75,12 +75,14 @@ def test_fp32_matches_reference(api, name):
     check(zscores(got, ref), f"{name} fp32")
 
 
-@pytest.mark.parametrize("name", ["linear_demo", "linear_sides_demo_ss"])
+@pytest.mark.parametrize("name", ["linear_demo", "linear_sides_demo_ss", "kinked_demo_120_35_spec"])
 def test_fp32_matches_reference_on_its_demo_models(api, name, tmp_path):
     """The reference's own demo models (psim_python/json/), against 16 seeded runs of the
     reference built from its current sources.  The result tables the reference commits for
     these models came from an older version of psim and lie several combined SE from its
-    current sources' runs; they are reported here, not used as the bar."""
+    current sources' runs; they are reported here, not used as the bar.  The kinked demo
+    (6174 cells, 3108 sensors) is larger than the shared-memory tables and tallies hold, so it
+    runs the transport kernel with global tables and global tally atomics."""
     gold = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))
     ref = gold["stats"].astype(np.float64)
     m = api.Model(demo_model_path(name, str(tmp_path)))
