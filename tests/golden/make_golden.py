@@ -368,7 +368,7 @@ def main():
     if only is None or "invert" in only:
         make_invert(paths)
     if not args.skip_runs and (only is None or "runs" in only):
-        make_runs(paths, [n for n in model_specs() if n != "bar_phasor"])
+        make_runs(paths, list(model_specs()))
     demo_paths = copy_demos(args.reference) if only is None or {"demos", "topology", "seeded"} & only else {}
     if only is None or "seeded" in only:
         make_demo_seeded(demo_paths)

@@ -64,7 +64,8 @@ def test_material_tables(O, name):
 
 
 @pytest.mark.parametrize("name,seeds", [("bar_ss", [1, 2]), ("bar_full", [3]), ("bar_periodic", [4]),
-                                        ("kinked_small", [5]), ("plate_small", [6]), ("bar_runs", [7])])
+                                        ("kinked_small", [5]), ("plate_small", [6]), ("bar_runs", [7]),
+                                        ("bar_phasor", [8])])
 def test_seeded_runs_match_reference(O, name, seeds):
     """Whole runs: with the reference's seed, the oracle reproduces its per-sensor results."""
     gold = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))
