@@ -68,7 +68,8 @@ def check(z, label):
     assert over3 <= allowed, (label, over3)
 
 
-@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "bar_periodic", "kinked_small", "plate_small", "bar_runs"])
+@pytest.mark.parametrize("name", ["bar_ss", "bar_full", "bar_periodic", "kinked_small", "plate_small", "bar_runs",
+                                  "bar_phasor"])
 def test_fp32_matches_reference(api, name):
     ref = np.load(os.path.join(GOLDEN, f"runs_{name}.npz"))["stats"]
     got = gpu_stats(api, name, api.FP32)
