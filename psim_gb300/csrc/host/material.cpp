@@ -2,6 +2,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <stdexcept>
+#include <string>
 
 #include "geom64.hpp"
 
@@ -89,7 +91,14 @@ std::array<double, kBins> MaterialTables::distribution(double T, int pol) const 
 }
 
 void MaterialTables::build_tables(double lo, double hi) {
-    const auto n = static_cast<std::size_t>((hi - lo) / static_cast<double>(kTempInterval));
+    const double span = (hi - lo) / static_cast<double>(kTempInterval);
+    if (!(span >= 0.) || !std::isfinite(span)) { throw std::invalid_argument("invalid temperature bounds for the material tables"); }
+    if (span >= static_cast<double>(kMaxTableTemps - 1)) {
+        throw std::length_error("the model's temperatures span more than "
+                                + std::to_string(static_cast<int>((kMaxTableTemps - 1) * static_cast<double>(kTempInterval)))
+                                + " K: its material tables (one per 0.1 K) would not fit in host memory");
+    }
+    const auto n = static_cast<std::size_t>(span);
     temps_.assign(n, 0.);
     double step = -1.;
     for (auto& t : temps_) { t = lo + static_cast<double>(kTempInterval) * (step += 1); }

@@ -18,6 +18,9 @@ constexpr std::size_t kBins = 1000;
 constexpr double kHbar = 1.054517e-34;
 constexpr double kBoltz = 1.38065e-23;
 constexpr float kTempInterval = .1F;// temperature grid step of the tables (psim/src/model.cpp:25)
+// Most grid temperatures one material's tables may hold: a 5000 K span at kTempInterval, about
+// 2.4 GB of host tables (three cumulative tables of 1000 (probability, LA fraction) pairs each).
+constexpr std::size_t kMaxTableTemps = 50001;
 
 enum Polar : int { kLA = 0, kTA = 1 };
 

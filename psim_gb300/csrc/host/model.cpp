@@ -244,6 +244,7 @@ void HostModel::add_cell(P2 p1, P2 p2, P2 p3, std::uint64_t sensor_id, double sp
 // Model::setEmitSurface / Cell::setEmitSurface / CompositeSurface::addEmitSurface
 // (psim/src/model.cpp:125-138, cell.cpp:29-35, compositeSurface.cpp:17-31)
 bool HostModel::set_emit(P2 p1, P2 p2, double temp, double duration, double start) {
+    if (!(temp > 0.) || !std::isfinite(temp)) { throw std::runtime_error("Emitting surface temperature must be positive and finite."); }
     if ((start < 0. || start >= sim_time_) || (duration < 0. || duration > sim_time_ - start)) {
         throw std::runtime_error("Transient Surface start_time or duration specifications are invalid.");
     }

@@ -292,6 +292,17 @@ def test_rate_inputs_are_refused_before_any_device_work(api, tmp_path):
         m["sensors"][1]["t_init"] = t
         with pytest.raises(api.PsimError, match="Sensor temperature"):
             api.Model(_write(str(tmp_path), m))
+    # the tables hold one temperature per 0.1 K between the model's lowest and highest: a span
+    # beyond the grid limit is a size error, found before anything is allocated
+    m = json.loads(json.dumps(base))
+    m["sensors"][1]["t_init"] = 1e12
+    with pytest.raises(api.PsimError, match="span more than 5000 K") as e:
+        api.Model(_write(str(tmp_path), m))
+    assert e.value.code == api.PSIM_ERR_LIMIT
+    m = json.loads(json.dumps(base))
+    m["emit_surfaces"][0]["temp"] = -5.0
+    with pytest.raises(api.PsimError, match="Emitting surface temperature"):
+        api.Model(_write(str(tmp_path), m))
     # the simulator seam takes the rate temperatures and coefficients from its caller
     model = api.Model(model_path("bar_ss"))
     d = model.sim_desc()
