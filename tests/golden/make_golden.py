@@ -3,6 +3,10 @@ sources (oracle/_ref/ref_driver, see oracle/ref_recipe/Makefile).  Run it where 
 reference tree is available:
 
     python tests/golden/make_golden.py [--reference /path/to/reference] [--skip-runs]
+        [--only geom,tables,invert,runs,topology,seeded,demos] [--demo <demo>[,<demo>]]
+
+The demo runs dominate: each of the 16 runs of kinked_demo_120_35_spec (6174 cells, a 2e7
+phonon budget, 6.2e9 phonon-steps) took about an hour of one host thread.
 
 Outputs (all small):
   models/*.json          the model files the fixtures were made from (psim_gb300.modelgen)
