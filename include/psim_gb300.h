@@ -350,6 +350,19 @@ int psim_geom_tri_contains(int64_t n, const double* tris, const double* pts, int
  * contains pts[i], or -1. */
 int psim_geom_edge_index(int64_t n, const double* tris, const double* pts, int32_t* out);
 
+/* ------------------------------------------------------------------------------------------
+ * The frequency sampler, for checks (host only, no GPU needed).
+ * ------------------------------------------------------------------------------------------ */
+/* Material::freqIndex (psim/src/material.cpp:64-75) draws bin h with the probability
+ * cum[h] - cum[h-1] of a cumulative table (bin 1 also takes bin 0's mass, bin 999 the rest
+ * above cum[998]) and LA with probability la_frac[h].  The kernels draw the same (bin,
+ * polarization) outcomes from the Walker alias table the engine builds from that table;
+ * this returns it.  table[1000][2] = (cumulative probability, LA fraction); out[2048], one word
+ * per column: acceptance threshold (21 bits) << 11 | alias column.  Outcome 2h is bin h LA,
+ * 2h + 1 bin h TA; a 32-bit random word picks column (word >> 21) and keeps it when
+ * (word & 0x1FFFFF) is below the threshold, else takes the alias. */
+int psim_sampling_alias_table(const double* table, uint32_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -149,6 +149,7 @@ SIGNATURES = {
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_edge_index": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
+    "psim_sampling_alias_table": (ctypes.c_int, [_c_dp, _c_u32p]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -559,4 +560,15 @@ def geom_edge_index(tris: np.ndarray, pts: np.ndarray) -> np.ndarray:
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     out = np.zeros(tris.shape[0], dtype=np.int32)
     _check(lib().psim_geom_edge_index(tris.shape[0], _dp(tris), _dp(pts), _i32(out)))
+    return out
+
+
+def alias_table(table: np.ndarray) -> np.ndarray:
+    """psim_sampling_alias_table: the alias table (uint32[2048]) the kernels sample (bin,
+    polarization) from, for one cumulative table [1000][2] = (cumulative probability, LA fraction)."""
+    table = np.ascontiguousarray(table, dtype=np.float64)
+    if table.shape != (1000, 2):
+        raise ValueError("a cumulative table is [1000][2]")
+    out = np.zeros(2048, dtype=np.uint32)
+    _check(lib().psim_sampling_alias_table(_dp(table), out.ctypes.data_as(_c_u32p)))
     return out

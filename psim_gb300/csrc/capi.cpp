@@ -2,6 +2,7 @@
 // exceptions and returns a status code; the message is kept per thread.
 #include "../../include/psim_gb300.h"
 
+#include <algorithm>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -607,6 +608,14 @@ int psim_geom_tri_contains(int64_t n, const double* tris, const double* pts, int
 int psim_geom_edge_index(int64_t n, const double* tris, const double* pts, int32_t* out) {
     if (n < 0 || (n > 0 && (tris == nullptr || pts == nullptr || out == nullptr))) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
     return guard([&]() { psim::gpu::geom_edge_index(n, tris, pts, out); });
+}
+
+int psim_sampling_alias_table(const double* table, uint32_t* out) {
+    if (table == nullptr || out == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
+    return guard([&]() {
+        const auto t = psim::gpu::alias_table_of(table);
+        std::copy(t.begin(), t.end(), out);
+    });
 }
 
 }// extern "C"

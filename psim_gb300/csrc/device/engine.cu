@@ -134,6 +134,8 @@ __global__ void unpack_kernel(const TallySlot* t, std::uint32_t S, std::uint64_t
 
 }// namespace
 
+std::vector<std::uint32_t> alias_table_of(const double* tab) { return alias_table(tab); }
+
 // Device cell records from the flattened description: the FP32 cell-local form (outward
 // normals, offsets, edge links, neighbour entry edges) and the FP64 reference form.
 void build_cells(const SimDesc& d, std::vector<CellF32>& c32, std::vector<CellF64>& c64, std::vector<Sub64>& subs) {

@@ -192,6 +192,9 @@ void geom_on_line(std::int64_t n, const double* lines, const double* pts, std::i
 void geom_tri_contains(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
 void geom_edge_index(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
 
+// The Walker alias table the engine uploads for one cumulative table (tab[1000][2]): 2048 words.
+std::vector<std::uint32_t> alias_table_of(const double* tab);
+
 int device_count() noexcept;
 // A non-blocking CUDA stream of the current device (as void*), and its release.
 void* create_stream();
