@@ -67,6 +67,9 @@ typedef struct psim_run_counters {
     uint64_t d2h_bytes;      /* device-to-host bytes copied by the last run and its read-outs */
     uint64_t transport_launches; /* launches of the phonon transport kernel (an FP32 launch covers several steps) */
     uint64_t steps_per_launch;   /* measurement steps per transport launch in the last run (FP64: 1) */
+    uint64_t backscatters;       /* phonons sent back at an interface between two materials because their
+                                    frequency exceeds the other material's branch maximum (last run) */
+    uint64_t state_bytes;        /* device bytes of the phonon state buffers the last run used */
 } psim_run_counters;
 
 /* InputManager::deserialize (psim/src/inputManager.cpp:14-115): reads and validates the model

@@ -48,7 +48,8 @@ class RunCounters(ctypes.Structure):
                 ("eff_energy", ctypes.c_double), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double),
                 ("max_population", ctypes.c_uint64), ("limit_hits", ctypes.c_uint64),
                 ("event_limit_hits", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
-                ("transport_launches", ctypes.c_uint64), ("steps_per_launch", ctypes.c_uint64)]
+                ("transport_launches", ctypes.c_uint64), ("steps_per_launch", ctypes.c_uint64),
+                ("backscatters", ctypes.c_uint64), ("state_bytes", ctypes.c_uint64)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}

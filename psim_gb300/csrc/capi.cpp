@@ -211,6 +211,8 @@ int psim_model_counters(const psim_model* m, psim_run_counters* out) {
     out->d2h_bytes = c.d2h_bytes;
     out->transport_launches = c.transport_launches;
     out->steps_per_launch = c.steps_per_launch;
+    out->backscatters = c.backscatters;
+    out->state_bytes = c.state_bytes;
     return PSIM_OK;
 }
 
@@ -358,6 +360,8 @@ int psim_sim_counters(const psim_sim* s, psim_run_counters* out) {
     out->d2h_bytes = c.d2h_bytes;
     out->transport_launches = c.transport_launches;
     out->steps_per_launch = c.steps_per_launch;
+    out->backscatters = c.backscatters;
+    out->state_bytes = c.state_bytes;
     return PSIM_OK;
 }
 

@@ -296,7 +296,8 @@ struct StepParams {
     std::uint32_t key0, key1;
     TallySlot* tally;                 // [n_recorded][n_sensors]
     unsigned long long* counters;     // [0] phonon-steps, [1] collision-limit relocations, [2] overflow,
-                                      // [3] max population, [4] event-limit hits, [5] staging timeouts
+                                      // [3] max population, [4] event-limit hits, [5] staging timeouts,
+                                      // [6] backscatters at interfaces between materials
 };
 
 }// namespace psim::gpu

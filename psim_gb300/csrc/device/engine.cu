@@ -58,7 +58,22 @@ struct Buf {
         if (!v.empty()) { check(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload"); }
     }
     template<typename T> T* as() const { return static_cast<T*>(p); }
+    // Takes over o's allocation (releasing its own).
+    void take(Buf& o) {
+        release();
+        p = o.p;
+        bytes = o.bytes;
+        o.p = nullptr;
+        o.bytes = 0;
+    }
 };
+
+// Phonon state of a run whose phonons all fit in this many bytes (two buffers) is sized for
+// every phonon of the run, and the run is one CUDA graph; larger runs are sized near their peak
+// population and grow between chunks of launches (Engine::run).
+constexpr std::uint64_t kWholeRunStateBytes = std::uint64_t{ 512 } << 20;
+// Transport launches per chunk of a chunked run.
+constexpr std::uint64_t kLaunchesPerChunk = 16;
 
 Line64 line64(psim::P2 a, psim::P2 b) {
     const psim::Seg64 s = psim::make_seg(a, b, nullptr);
@@ -583,18 +598,49 @@ void Engine::run(int precision, void* stream_ptr) {
     cudaStream_t stream = stream_ptr != nullptr ? static_cast<cudaStream_t>(stream_ptr) : I.own;
     const bool fp64 = precision != 0;
     const std::size_t rec_bytes = fp64 ? 64 : 32;
-    // Capacity: the population never exceeds the number of phonons created in the run.
-    std::uint64_t want = std::max<std::uint64_t>(I.total + 1024, 4096);
-    std::size_t free_b = 0;
-    std::size_t total_b = 0;
-    check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-    const std::uint64_t limit = static_cast<std::uint64_t>(free_b * 0.8) / (2 * rec_bytes);
-    if (want > limit) { want = limit; }
-    if (I.capacity < want || I.state[0].bytes < want * rec_bytes) {
-        I.state[0].alloc(want * rec_bytes);
-        I.state[1].alloc(want * rec_bytes);
-        I.capacity = want;
+    // State buffers.  The population never exceeds the phonons created in the run, so a run whose
+    // phonons all fit in kWholeRunStateBytes gets room for every one of them and runs as one CUDA
+    // graph.  A larger run is chunked instead: before each chunk of launches the host reads the
+    // population entering it and grows the buffers when that population plus the chunk's newborns
+    // would not fit, so the buffers follow the peak population and no phonon is ever dropped.
+    const std::uint64_t whole = std::max<std::uint64_t>(I.total + 1024, 4096);
+    const bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
+    if (I.state[0].bytes != I.capacity * rec_bytes) {// first run, or the other precision's records
+        I.state[0].release();
+        I.state[1].release();
+        I.capacity = 0;
     }
+    // Room for at least 'need' phonons; 'live' records of the buffer 'cur' are kept.
+    auto ensure_capacity = [&](std::uint64_t need, std::uint64_t live, int cur) {
+        if (need <= I.capacity) { return; }
+        if (need > 0xFFFFFFFFULL) { throw std::length_error("more than 2^32 - 1 phonons in flight"); }
+        std::size_t free_b = 0;
+        std::size_t total_b = 0;
+        check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        const std::uint64_t held = I.capacity * 2 * rec_bytes;
+        const std::uint64_t limit = static_cast<std::uint64_t>((free_b + held) * 0.8) / (2 * rec_bytes);
+        std::uint64_t cap = chunked ? std::max(need + need / 4, I.capacity + I.capacity / 2) : need;
+        cap = std::min<std::uint64_t>(std::min(cap, limit), 0xFFFFFFFFULL);
+        if (cap < need) {
+            throw std::length_error("phonon buffers: " + std::to_string(need) + " phonons in flight do not fit in device memory");
+        }
+        Buf a;
+        Buf b;
+        a.alloc(cap * rec_bytes);
+        b.alloc(cap * rec_bytes);
+        if (live > 0) {// records are SoA: one 16-byte word per phonon per segment of 'capacity' words
+            for (std::size_t k = 0; k < rec_bytes / 16; ++k) {
+                check(cudaMemcpyAsync(static_cast<char*>(a.p) + k * cap * 16, static_cast<const char*>(I.state[cur].p) + k * I.capacity * 16,
+                                      live * 16, cudaMemcpyDeviceToDevice, stream),
+                      "state copy");
+            }
+            check(cudaStreamSynchronize(stream), "state copy");
+        }
+        I.state[cur].take(a);
+        I.state[1 - cur].take(b);
+        I.capacity = cap;
+    };
+    if (!chunked) { ensure_capacity(whole, 0, 0); }
     check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
     check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
     check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
@@ -704,6 +750,7 @@ void Engine::run(int precision, void* stream_ptr) {
     std::uint64_t launches = 0;
     std::uint64_t w = 0;
     auto enqueue = [&](std::uint64_t from, std::uint64_t to) {
+        P.capacity = static_cast<std::uint32_t>(I.capacity);
         for (std::uint64_t s0 = from; s0 < to; ++w) {
             std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, to - s0));
             // every work item of a launch is numbered in 32 bits
@@ -753,19 +800,32 @@ void Engine::run(int precision, void* stream_ptr) {
     steps_run_ = d.steps;
 
     check(cudaEventRecord(I.ev0, stream), "event record");
-    if (stop_on_) {// launches in chunks, the recorded steps checked for steady state after each
-        if (d.step_adj != 0 || d.recorded != d.steps) {
+    if (chunked) {// launches in chunks: buffers grown between chunks, steady-state checks where asked
+        if (stop_on_ && (d.step_adj != 0 || d.recorded != d.steps)) {
             throw std::invalid_argument("stopping at steady state needs every step recorded (periodic or transient runs)");
         }
         const std::uint64_t min_steps = static_cast<std::uint64_t>(stop_crit_.patience + 1) * stop_crit_.window;
         const std::uint64_t every = stop_check_ > 0 ? stop_check_ : min_steps;
+        std::vector<std::uint64_t> born(d.steps + 1, 0);// newborns of steps [0, s)
+        for (std::uint64_t s = 0; s < d.steps; ++s) { born[s + 1] = born[s] + I.n_new[s]; }
         std::uint64_t done = 0;
+        // steady checks at the multiples of 'every' from min_steps on
+        std::uint64_t next_check = stop_on_ ? std::max<std::uint64_t>(1, (min_steps + every - 1) / every) * every : d.steps;
         while (done < d.steps) {
-            const std::uint64_t to = std::min<std::uint64_t>(d.steps, done + every);
+            std::uint64_t to = std::min<std::uint64_t>(d.steps, done + kLaunchesPerChunk * fused);
+            if (stop_on_) { to = std::min(to, next_check); }
+            // the phonons entering step 'done' (the next launch's input count) plus the chunk's newborns
+            std::uint32_t live = 0;
+            if (done > 0) {
+                check(cudaMemcpyAsync(&live, counts + (w % 3), sizeof live, cudaMemcpyDeviceToHost, stream), "count read");
+                check(cudaStreamSynchronize(stream), "count read");
+            }
+            ensure_capacity(static_cast<std::uint64_t>(live) + (born[to] - born[done]) + 1024, live, static_cast<int>(w % 2));
             enqueue(done, to);
             check(cudaGetLastError(), "step launch");
             done = to;
-            if (done < d.steps && done >= min_steps) {
+            if (stop_on_ && done == next_check && done < d.steps) {
+                next_check = std::min<std::uint64_t>(d.steps, done + every);
                 ++checks;
                 if (steady_onset_device(I.tally.p, d.n_sensors, done, stop_crit_, nullptr, stream) >= 0) { break; }
             }
@@ -802,6 +862,8 @@ void Engine::run(int precision, void* stream_ptr) {
     counters_.phonon_steps += c[0];
     counters_.relocations += c[1];
     counters_.event_limits += c[4];
+    counters_.backscatters += c[6];
+    counters_.state_bytes = I.state[0].bytes + I.state[1].bytes;
     if (c[5] != 0) { throw std::runtime_error("CUDA staging of the model tables into shared memory timed out"); }
     counters_.overflow += c[2];
     counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);

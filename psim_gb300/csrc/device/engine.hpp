@@ -55,6 +55,8 @@ struct RunCounters {
     std::uint64_t d2h_bytes{ 0 };
     std::uint64_t transport_launches{ 0 };
     std::uint64_t steps_per_launch{ 0 };
+    std::uint64_t backscatters{ 0 };
+    std::uint64_t state_bytes{ 0 };
     double kernel_ms{ 0. };
 };
 

@@ -368,7 +368,8 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
                     L.changed = true;
                 }
                 L.mat = C->material;
-            } else {
+            } else {// backscatter: no state of this frequency in the neighbour's material
+                atomicAdd(P.counters + 6, 1ULL);
                 const float flip = ((C->rev >> (8 + ebest)) & 1U) ? -1.f : 1.f;
                 diffuse_dir(p, rs, -E.x * flip, -E.y * flip);
             }

@@ -140,6 +140,7 @@ __device__ bool collide64(const StepParams& P, Ph64& p, Stream& rs, psim::P2 poi
                 const MaterialDev& mt = P.materials[n.material];
                 const double max_freq = (meta_pol(p.meta) == 0) ? mt.w_max_la64 : mt.w_max_ta64;
                 if (p.w > max_freq) {
+                    atomicAdd(P.counters + 6, 1ULL);
                     diffuse_dir(p, rs, s.nx, s.ny);
                 } else {
                     p.meta = meta_with_cell_edge(p.meta, s.target, kNoEdge);

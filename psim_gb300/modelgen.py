@@ -60,6 +60,22 @@ SILICON = {
     "r_data": {"b_l": 2.0e-24, "b_tn": 9.3e-13, "b_tu": 5.5e-18, "b_i": 1.2e-45, "w": 2.417e13},
 }
 
+# Germanium: the dispersion and relaxation set psim ships beside silicon
+# (psim_python/psim/pre_builts.py:25-29).  Its branch maxima lie below silicon's, so a
+# silicon phonon above them is backscattered at a Si|Ge interface
+# (TransitionSurface::handlePhonon, psim/src/surface.cpp:71-109); its impurity
+# coefficient is zero.
+GERMANIUM = {
+    "name": "Germanium",
+    "d_data": {
+        "la_data": [-1.50e-7, 5.63e3, 0.0],
+        "max_freq_la": 4.45236386e13,
+        "ta_data": [-1.13e-7, 2.60e3, 0.0],
+        "max_freq_ta": 1.4937724175e13,
+    },
+    "r_data": {"b_l": 2.3e-24, "b_tn": 30.0e-13, "b_tu": 1.5e-18, "b_i": 0.0, "w": 1.23e13},
+}
+
 
 class Builder:
     """Accumulates sensors, cells and emitting surfaces in psim's JSON layout."""
@@ -78,13 +94,19 @@ class Builder:
             "phasor_sim": bool(phasor_sim),
         }
         self.material = material
+        self.materials: List[dict] = [material]
         self.sensors: List[dict] = []
         self.cells: List[dict] = []
         self.surfaces: List[dict] = []
 
-    def add_sensor(self, t_init: float) -> int:
+    def add_sensor(self, t_init: float, material: dict = None) -> int:
+        """A sensor of ``material`` (the builder's material by default; another one is added
+        to the model's material list on first use)."""
+        mat = self.material if material is None else material
+        if all(m["name"] != mat["name"] for m in self.materials):
+            self.materials.append(mat)
         sid = len(self.sensors)
-        self.sensors.append({"id": sid, "material": self.material["name"], "t_init": float(t_init)})
+        self.sensors.append({"id": sid, "material": mat["name"], "t_init": float(t_init)})
         return sid
 
     def add_triangle(self, p1: Point, p2: Point, p3: Point, sensor: int, spec: float) -> None:
@@ -113,7 +135,7 @@ class Builder:
     def to_dict(self) -> dict:
         # ModelBuilder sorts surfaces by decreasing 'length' before export.
         surfaces = sorted(self.surfaces, key=lambda s: s["length"], reverse=True)
-        return {"settings": dict(self.settings), "materials": [self.material], "sensors": self.sensors,
+        return {"settings": dict(self.settings), "materials": list(self.materials), "sensors": self.sensors,
                 "cells": self.cells, "emit_surfaces": surfaces}
 
 
@@ -134,6 +156,24 @@ def bar(*, num_cells: int = 10, length: float = 1000.0, width: float = 100.0, t_
     dx = length / num_cells
     for i in range(num_cells):
         s = b.add_sensor(t_init)
+        b.add_rectangle((i * dx, 0.0), ((i + 1) * dx, width), s, spec)
+    b.add_surface((0.0, 0.0), (0.0, width), t_left)
+    b.add_surface((length, 0.0), (length, width), t_right)
+    return b.to_dict()
+
+
+def two_material_bar(*, num_cells: int = 10, split: int = 5, length: float = 1000.0, width: float = 100.0,
+                     t_left: float = 310.0, t_right: float = 290.0, t_init: float = 300.0, t_eq: float = 300.0,
+                     spec: float = 0.0, num_measurements: int = 1000, sim_time: float = 5.0,
+                     num_phonons: int = 100000, sim_type: int = 0, step_interval: int = 0,
+                     left: dict = SILICON, right: dict = GERMANIUM) -> dict:
+    """The bar of ``bar`` with its first ``split`` cells of material ``left`` and the rest of
+    ``right``: one interface between two materials, crossed by phonons both ways."""
+    b = Builder(num_measurements=num_measurements, sim_time=sim_time, num_phonons=num_phonons, t_eq=t_eq,
+                sim_type=sim_type, step_interval=step_interval, material=left)
+    dx = length / num_cells
+    for i in range(num_cells):
+        s = b.add_sensor(t_init, left if i < split else right)
         b.add_rectangle((i * dx, 0.0), ((i + 1) * dx, width), s, spec)
     b.add_surface((0.0, 0.0), (0.0, width), t_left)
     b.add_surface((length, 0.0), (length, width), t_right)

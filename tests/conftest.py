@@ -33,7 +33,15 @@ def gpu(built):
 
 
 def model_path(name: str) -> str:
-    return os.path.join(GOLDEN, "models", name + ".json")
+    """A fixture model file: tests/golden/models/<name>.json, or its gzipped form written out
+    as plain JSON into a per-user temporary directory."""
+    plain = os.path.join(GOLDEN, "models", name + ".json")
+    if os.path.exists(plain) or not os.path.exists(plain + ".gz"):
+        return plain
+    import tempfile
+    directory = os.path.join(tempfile.gettempdir(), f"psim_gb300_models_{os.getuid()}")
+    os.makedirs(directory, exist_ok=True)
+    return demo_model_path(name, directory)
 
 
 def demo_model_path(name: str, directory: str) -> str:

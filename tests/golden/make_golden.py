@@ -2,8 +2,9 @@
 sources (oracle/_ref/ref_driver, see oracle/ref_recipe/Makefile).  Run it where the
 reference tree is available:
 
-    python tests/golden/make_golden.py [--reference /path/to/reference] [--skip-runs]
-        [--only geom,tables,invert,runs,topology,seeded,demos] [--demo <demo>[,<demo>]]
+    python tests/golden/make_golden.py --reference /path/to/reference [--skip-runs]
+        [--only geom,tables,invert,runs,topology,seeded,demos,headline,headline_tables,headline_topology]
+        [--demo <demo>[,<demo>]]
 
 The demo runs dominate: each of the 16 runs of kinked_demo_120_35_spec (6174 cells, a 2e7
 phonon budget, 6.2e9 phonon-steps) took about an hour of one host thread.
@@ -64,12 +65,51 @@ def model_specs():
     }
 
 
+def headline_specs():
+    """The benchmark configurations as they are stated: geometry, mode, step length and number
+    of steps of each, at its own phonon budget where the reference runs 16 seeds in minutes,
+    else at a reduced one (the per-sensor means of a deviational run do not depend on the
+    budget; only their noise does).
+
+    cfg0_bar_ss     1 um x 100 nm bar, 10 cells, 310/290 K, deviational steady state, 2000
+                    steps of 5 ps, 2e5 phonons per step (budget 3.09e6 at a mean lifetime
+                    of 129.5 steps)
+    cfg2b_bar_full  the same bar in full mode at 60/40 K (budget 2.04e6, lifetime 196 steps)
+    cfg1_kinked     the 400-sensor kinked structure, periodic, 5000 steps of 2 ps, output
+                    every 50 steps; budget 6e6 instead of the 1.2e8 of 1e7 per step
+    cfg2a_plate     the 4 x 1 um plate, 64 x 16 cells, transient 20 ps pulse, 3000 steps of
+                    1 ps; budget 5e5 instead of 2e7
+    si_ge_bar       the bar with five silicon and five germanium cells: one interface between
+                    two materials (germanium from psim_python/psim/pre_builts.py:25-29)
+    """
+    return {
+        "cfg0_bar_ss": mg.bar(num_phonons=3090000, num_measurements=2000, sim_time=10.0),
+        "cfg2b_bar_full": mg.bar(num_phonons=2040000, num_measurements=2000, sim_time=10.0, t_eq=0.0, t_left=60.0,
+                                 t_right=40.0, t_init=50.0),
+        "cfg1_kinked": mg.kinked(seed=0, num_measurements=5000, sim_time=10.0, step_interval=50, num_phonons=6000000),
+        "cfg2a_plate": mg.plate(num_phonons=500000),
+        "si_ge_bar": mg.two_material_bar(num_phonons=300000, num_measurements=1000, sim_time=5.0),
+    }
+
+
+GZIPPED = {"cfg1_kinked", "cfg2a_plate"}  # larger model files are kept gzipped
+
+
 def write_models():
     os.makedirs(MODELS, exist_ok=True)
     paths = {}
     for name, m in model_specs().items():
         p = os.path.join(MODELS, name + ".json")
         mg.write(m, p)
+        paths[name] = p
+    td = tempfile.mkdtemp(prefix="psim_headline_")
+    for name, m in headline_specs().items():
+        if name in GZIPPED:
+            p = mg.write(m, os.path.join(td, name + ".json"))
+            with open(p, "rb") as f, gzip.GzipFile(os.path.join(MODELS, name + ".json.gz"), "wb", mtime=0) as g:
+                g.write(f.read())
+        else:
+            p = mg.write(m, os.path.join(MODELS, name + ".json"))
         paths[name] = p
     return paths
 
@@ -186,6 +226,28 @@ def make_geom():
 
 
 # ---------------------------------------------------------------- tables
+def make_tables_two_materials(paths, name="si_ge_bar"):
+    """tables_<name>.npz for a model of two materials: each material's frequency grid,
+    velocities, densities of states and every temperature's sums, with full tables at three
+    temperatures (prefix m0_ / m1_ in the model's material order)."""
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "t.bin")
+        driver("tables", paths[name], out)
+        mats, bounds = read_tables(out, n_materials=2)
+    arrays = {"bounds": bounds}
+    for i, m in enumerate(mats):
+        nt = len(m["temps"])
+        keep = sorted(set([0, nt // 2, nt - 1] + [int(np.searchsorted(m["temps"], t)) for t in (300.0, 310.0, 290.0)
+                                                  if m["temps"][0] <= t <= m["temps"][-1]]))
+        for k in ("temps", "freq", "vel_la", "vel_ta", "dens_la", "dens_ta", "base_sum", "emit_sum", "scatter_sum"):
+            arrays[f"m{i}_{k}"] = m[k]
+        arrays[f"m{i}_keep"] = np.array(keep)
+        for k in ("base", "emit", "scatter"):
+            arrays[f"m{i}_{k}"] = m[k][keep]
+    np.savez_compressed(os.path.join(HERE, f"tables_{name}.npz"), **arrays)
+    print(f"tables_{name}.npz: {[len(m['temps']) for m in mats]} temperatures")
+
+
 def make_tables(paths):
     for name in ("bar_ss", "bar_full", "kinked_small"):
         with tempfile.TemporaryDirectory() as td:
@@ -284,14 +346,18 @@ def ref_run(path, seed):
     return acc / len(runs), d["total_phonons_last_run"]
 
 
-def make_runs(paths, names):
+def make_runs(paths, names, single=False):
+    """runs_<name>.npz: 16 seeded reference runs per model.  ``single`` stores float32 (larger
+    tables; the seed-to-seed spreads lie far above its resolution)."""
     for name in names:
         with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as pool:
             res = list(pool.map(lambda s: ref_run(paths[name], s), SEEDS))
         stats = np.stack([r[0] for r in res])
         phonons = np.array([r[1] for r in res])
+        if single:
+            stats = stats.astype(np.float32)
         np.savez_compressed(os.path.join(HERE, f"runs_{name}.npz"), seeds=np.array(SEEDS), stats=stats, phonons=phonons)
-        print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}")
+        print(f"runs_{name}.npz: {stats.shape}, mean T {stats[:, :, 0].mean(axis=0)[:4]}", flush=True)
 
 
 # ---------------------------------------------------------------- the reference's own demo models
@@ -355,7 +421,7 @@ def make_demo_seeded(paths):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the reference checkout (the psim project)")
     ap.add_argument("--skip-runs", action="store_true")
     ap.add_argument("--only", default="")
     ap.add_argument("--demo", default="", help="comma-separated demo models for the demo runs (default: all three)")
@@ -373,6 +439,14 @@ def main():
         make_invert(paths)
     if not args.skip_runs and (only is None or "runs" in only):
         make_runs(paths, list(model_specs()))
+    if only is None or "headline_tables" in only:
+        make_tables_two_materials(paths)
+    if only is None or "headline_topology" in only:
+        make_topology({k: paths[k] for k in headline_specs()})
+    if not args.skip_runs and (only is None or "headline" in only):
+        # quickest first, so that the fixtures arrive as they are done
+        make_runs(paths, ["si_ge_bar", "cfg2b_bar_full", "cfg0_bar_ss"])
+        make_runs(paths, ["cfg2a_plate", "cfg1_kinked"], single=True)
     demo_paths = copy_demos(args.reference) if only is None or {"demos", "topology", "seeded"} & only else {}
     if only is None or "seeded" in only:
         make_demo_seeded(demo_paths)

@@ -111,6 +111,55 @@ def test_tables_match_reference(api, name):
     assert (idesc.lower_bound, idesc.upper_bound) == tuple(gold["bounds"])
 
 
+def test_tables_of_two_materials_match_reference(api):
+    """A model of two materials (silicon and germanium cells): each material's frequency grid,
+    velocities and temperature sums, and the cumulative tables each sensor and emitter uses,
+    equal the reference's (Material::Material and initializeTables per material,
+    psim/src/material.cpp:20-51,101-204; Model::initializeMaterialTables)."""
+    gold = np.load(os.path.join(GOLDEN, "tables_si_ge_bar.npz"))
+    m = api.Model(model_path("si_ge_bar"))
+    d = m.sim_desc()
+    assert d.n_materials == 2
+    tabs = m.tables()
+    exact = os.uname().machine == "x86_64"
+
+    def same(a, b):
+        a = np.nan_to_num(a, nan=-1.0)
+        b = np.nan_to_num(b, nan=-1.0)
+        return np.array_equal(a, b) if exact else np.allclose(a, b, rtol=1e-12, atol=0)
+
+    S = d.n_sensors
+    st = np.ctypeslib.as_array(d.sensor_temp, shape=(S,))
+    smat = np.ctypeslib.as_array(d.sensor_material, shape=(S,))
+    base_idx = np.ctypeslib.as_array(d.sensor_base_table, shape=(S,))
+    scat_idx = np.ctypeslib.as_array(d.sensor_scatter_table, shape=(S,))
+    freq = np.ctypeslib.as_array(d.mat_freq, shape=(2, 1000))
+    vel = np.ctypeslib.as_array(d.mat_vel, shape=(2, 2, 1000))
+    idesc = m.interp_desc()
+    begin = [idesc.mat_temp_begin[i] for i in range(3)]
+    all_temps = np.ctypeslib.as_array(idesc.temps, shape=(begin[2],))
+    all_energies = np.ctypeslib.as_array(idesc.energies, shape=(begin[2],))
+    checked = 0
+    for i in range(2):
+        temps = gold[f"m{i}_temps"]
+        keep = list(gold[f"m{i}_keep"])
+        assert same(freq[i], gold[f"m{i}_freq"])
+        assert same(vel[i, 0], gold[f"m{i}_vel_la"]) and same(vel[i, 1], gold[f"m{i}_vel_ta"])
+        assert np.array_equal(all_temps[begin[i]:begin[i + 1]], temps)
+        assert same(all_energies[begin[i]:begin[i + 1]], gold[f"m{i}_base_sum"])
+        for s in np.nonzero(smat == i)[0]:
+            ti = int(np.searchsorted(temps, st[s]))
+            if ti in keep:
+                k = keep.index(ti)
+                assert same(tabs[base_idx[s]], gold[f"m{i}_base"][k])
+                assert same(tabs[scat_idx[s]], gold[f"m{i}_scatter"][k])
+                checked += 1
+    # the two materials' grids differ (germanium's branch maxima lie below silicon's)
+    assert freq[1, -1] < freq[0, -1]
+    assert checked >= 2
+    assert (idesc.lower_bound, idesc.upper_bound) == tuple(gold["bounds"])
+
+
 @pytest.mark.parametrize("name", ["bar_ss", "bar_full", "kinked_small"])
 def test_energy_per_phonon_matches_reference(api, name):
     """Model::getTotalInitialEnergy / num_phonons (model.cpp:148-155,196-201)."""
