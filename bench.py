@@ -177,8 +177,10 @@ def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
                             t_eq=0.0, num_measurements=2000, sim_time=10.0, num_phonons=n)
     n0 = budget(bar0, 2e5, 2000)
     cases = [
-        ("bar_steady_state", "1000 x 100 nm bar, 10 cells, deviational steady state, ends 310/290 K, 2e5 phonons per "
-                             "step, dt 5 ps, 2000 steps", bar0(n0), bar0(n0 // 4)),
+        ("bar_steady_state_fp64", "1000 x 100 nm bar, 10 cells, deviational steady state, ends 310/290 K, 2e5 phonons "
+                                  "per step, dt 5 ps, 2000 steps, FP64 kernel (the configuration's stated precision)",
+         bar0(n0), bar0(n0 // 4)),
+        ("bar_steady_state", "the same bar with the FP32 kernel (CPU oracle: the row above)", bar0(n0), False),
         ("bar_full_mode", "the same bar in full (non-deviational) mode, ends 60/40 K, 2e5 phonons per step, dt 5 ps, "
                           "2000 steps", full(budget(full, 2e5, 2000)), None),
         ("plate_transient", "4 x 1 um plate, 64 x 16 cells, transient, 400 K pulse on a 200 nm strip of the left edge "
@@ -186,19 +188,21 @@ def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
     ]
     out = {}
     for key, text, model, sample in cases:
+        prec = api.FP64 if key.endswith("_fp64") else precision
         path = mg.write(model, os.path.join(td, key + ".json"))
         m = api.Model(path)
-        m.run(seed=1, precision=precision)  # warm-up: tables, graph
+        m.run(seed=1, precision=prec)  # warm-up: tables, graph
         t0 = time.perf_counter()
-        m.run(seed=2, precision=precision)
+        m.run(seed=2, precision=prec)
         m.measurements()
         wall = time.perf_counter() - t0
         c = m.counters()
         m.close()
         row = {"workload": text, "num_phonons": model["settings"]["num_phonons"], "phonon_steps": c["phonon_steps"],
                "value": c["phonon_steps"] / (c["kernel_ms"] / 1e3), "e2e": c["phonon_steps"] / wall,
-               "unit": "phonon-steps/s", "mean_population": c["phonon_steps"] / model["settings"]["num_measurements"]}
-        if cpu:
+               "unit": "phonon-steps/s", "mean_population": c["phonon_steps"] / model["settings"]["num_measurements"],
+               "precision": "fp64" if prec == api.FP64 else "fp32"}
+        if cpu and sample is not False:
             from oracle import oracle
             cpath = path if sample is None else mg.write(sample, os.path.join(td, key + "_sample.json"))
             r = oracle.run(cpath, 5, threads=threads)
@@ -224,6 +228,28 @@ def precision_error(s32: np.ndarray, s64: np.ndarray) -> dict:
             out.update({"mean_abs_diff_K": row["mean_abs_diff"], "max_abs_diff_K": row["max_abs_diff"],
                         "seed_to_seed_sd_K": noise, "mean_diff_over_sd": row["mean_diff_over_sd"]})
         out[name] = row
+    return out
+
+
+def summarize_extras(steady, fp64_check, batch, warm, others) -> dict:
+    """The headline figures of the extra measurements, small enough for the headline line (the
+    full records are printed on their own lines before it)."""
+    out = {}
+    if steady is not None:
+        out["steady_onset_step"] = steady["onset_step"]
+    if fp64_check is not None:
+        out["fp32_vs_fp64_T"] = {k: fp64_check[k] for k in ("mean_abs_diff_K", "max_abs_diff_K", "seed_to_seed_sd_K")}
+    if batch is not None:
+        out["batch"] = {"value": batch["value"], "models": batch.get("models"), "alive_at_once": batch.get("alive_at_once"),
+                        "one_at_a_time": (batch.get("one_at_a_time") or {}).get("value")}
+    if warm is not None:
+        keep = ("mean_onset_steps_cold", "mean_onset_steps_warm", "steps_ratio_cold_over_warm",
+                "wall_ratio_cold_over_warm_to_steady_stop", "test_rmse_K", "stopped_within_3se_cold",
+                "stopped_within_3se_warm", "held_out_models", "train_fields")
+        out["warm_start"] = {k: warm[k] for k in keep if k in warm}
+    if others is not None:
+        out["other_workloads"] = {k: {"value": v["value"], "e2e": v["e2e"], "precision": v["precision"],
+                                      "cpu": (v.get("cpu_oracle") or {}).get("value")} for k, v in others.items()}
     return out
 
 
@@ -347,9 +373,14 @@ def main():
     barrier(dist)
     span_ms = ev0.elapsed_time(ev1)
     kernel_s = reduce_max(dist, kernel_ms / 1e3)
+    span_s = reduce_max(dist, span_ms / 1e3)
     total_steps = reduce_sum(dist, float(phonon_steps))
-    value = total_steps / kernel_s
-    ms_per_step = 1e3 * reduce_max(dist, span_ms / 1e3) / args.steps
+    # value: phonon-steps over the CUDA-event span of the K timed runs (host work between runs,
+    # births, graph set-up and buffer checks included); kernel_value: over the transport
+    # kernels' own device time
+    value = total_steps / span_s
+    kernel_value = total_steps / kernel_s
+    ms_per_step = 1e3 * span_s / args.steps
 
     # roofline of the dominant kernel (the FP32/FP64 transport step): 64 B per phonon-step (one
     # 32-byte state record read and one written) times the phonon-steps one launch covers; an FP32
@@ -491,6 +522,13 @@ def main():
                          f"on {threads} host threads with the CPU oracle"}
 
     if rank == 0:
+        # the extra measurements in full, one short JSON line each, before the headline line
+        details = {"steady_state": steady, "fp32_vs_fp64": fp64_check, "batch": batch, "warm_start": warm}
+        if others is not None:
+            details.update({f"other_workloads.{k}": v for k, v in others.items()})
+        for key, v in details.items():
+            if v is not None:
+                print(json.dumps({"detail": key, **v}), flush=True)
         line = {
             "metric": "phonon-steps/s", "value": value, "unit": "phonon-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -501,10 +539,12 @@ def main():
                        "mean_population": phonon_steps / args.steps / steps_n,
                        "l2": "inputs larger than L2 (phonon state 2 x 32 B x population)",
                        "precision": args.precision, "bench_step": "one full simulation run",
-                       "steps_per_launch": c["steps_per_launch"]},
+                       "steps_per_launch": c["steps_per_launch"], "state_bytes": c["state_bytes"]},
+            "value_source": "phonon-steps / CUDA-event span of the timed runs",
+            "kernel_value": kernel_value,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches * world,
-            "clocks": clk, "wall_s_timed": wall, "steady_state": steady, "fp32_vs_fp64": fp64_check, "batch": batch,
-            "warm_start": warm, "other_workloads": others,
+            "clocks": clk, "wall_s_timed": wall,
+            "extras": summarize_extras(steady, fp64_check, batch, warm, others),
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -90,6 +90,12 @@ int psim_model_shape(const psim_model* m, int64_t* n_sensors, int64_t* n_recorde
 int psim_model_measurements(const psim_model* m, double* stats);
 /* Per-step series of one run: temps[S][K] and fluxes[S][K][2] (SensorMeasurements::final_*). */
 int psim_model_series(const psim_model* m, int64_t run, double* temps, double* fluxes);
+/* OutputManager::addMeasurement for every sensor of `runs` runs (psim/src/outputManager.cpp:116-118):
+ * replaces the model's per-run results with statistics made elsewhere, stats[runs][S][6] (T, SE,
+ * flux x, SE, flux y, SE per sensor), for example runs combined from several processes.
+ * psim_model_measurements and psim_model_export then report them; they carry no per-step series,
+ * so a periodic export of them fails with PSIM_ERR_INVALID. */
+int psim_model_set_measurements(psim_model* m, const double* stats, int64_t runs);
 /* Raw tallies of the last run: energy[S][K] (sum of phonon signs) and flux[S][K][2]
  * (sum of sign * velocity, m/s) as Sensor::inc_energy_ / inc_flux_ (psim/src/sensor.cpp:43-52). */
 int psim_model_tallies(const psim_model* m, int64_t* energy, double* flux);
@@ -352,6 +358,19 @@ int psim_geom_tri_contains(int64_t n, const double* tris, const double* pts, int
 /* Cell::handleSurfaceCollision edge choice: index (0..2) of the first edge of tris[i] whose line
  * contains pts[i], or -1. */
 int psim_geom_edge_index(int64_t n, const double* tris, const double* pts, int32_t* out);
+
+/* ------------------------------------------------------------------------------------------
+ * Scattering rates on the GPU, for checks.
+ * ------------------------------------------------------------------------------------------ */
+/* Material::relaxRates(temp, freq, polarization) (psim/src/material.cpp:54-62,207-239) as the
+ * transport kernels evaluate it: out[n][3] = normal, Umklapp and impurity rates (1/s) of one
+ * material for the cases (T[i] K, freq[i] rad/s, pol[i] 0 LA / 1 TA).  mat_params holds the
+ * material as psim_sim_desc.mat_params does: b_l, b_tn, b_tu, b_i, w, bin width, w_max LA,
+ * w_max TA.  precision PSIM_PRECISION_FP32 takes the FP32 kernel's rate function (frequency
+ * rounded to float in units of 1e13 rad/s, temperature factors rounded to float as each
+ * sensor's are), PSIM_PRECISION_FP64 the FP64 kernel's.  At most 2^24 cases per call. */
+int psim_rates(const double* mat_params, int64_t n, const double* T, const double* freq, const int32_t* pol,
+               int precision, double* out);
 
 /* ------------------------------------------------------------------------------------------
  * The frequency sampler, for checks (host only, no GPU needed).

@@ -13,6 +13,8 @@
 //   geom   <cases.txt> <out.txt>                         geometry known answers
 //   invert <model.json> <counts.txt> <out.txt>           E->T inversion of given counts
 //   topology <model.json> <out.txt>                      assembled cells and edge sub-surfaces
+//   rates  <model.json> <cases.bin> <out.bin>            Material::relaxRates of every material on
+//                                                        given (T, frequency, polarization) triples
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -379,11 +381,33 @@ int cmdTopology(const std::string& model_path, const std::string& out_path) {
     return 0;
 }
 
+// Material::relaxRates(temp, freq, polar) (psim/src/material.cpp:54-62,207-239) of every
+// material of the model, in JSON order, on the cases in 'cases_path': float64 triples (T, freq,
+// polarization 0 LA / 1 TA).  Writes [material][case][N, U, I] float64.
+int cmdRates(const std::string& model_path, const std::string& cases_path, const std::string& out_path) {
+    const Value j = psim_json::parse_file(model_path);
+    auto model = buildModel(j);
+    std::ifstream is(cases_path, std::ios::binary);
+    std::vector<double> cases;
+    double v = 0.;
+    while (is.read(reinterpret_cast<char*>(&v), sizeof v)) { cases.push_back(v); }
+    std::ofstream os(out_path, std::ios::binary);
+    for (const Value& m : j.at("materials").items()) {
+        const Material& mat = model->materials_.at(m.at("name").as_string());
+        for (std::size_t i = 0; i + 2 < cases.size(); i += 3) {
+            const auto pol = cases[i + 2] == 0. ? Material::Polar::LA : Material::Polar::TA;
+            const auto r = mat.relaxRates(cases[i], cases[i + 1], pol);
+            for (double x : r) { os.write(reinterpret_cast<const char*>(&x), sizeof x); }
+        }
+    }
+    return 0;
+}
+
 }// namespace
 
 int main(int argc, char** argv) {
     if (argc < 2) {
-        std::cerr << "usage: ref_driver run|tables|geom|invert|topology ...\n";
+        std::cerr << "usage: ref_driver run|tables|geom|invert|topology|rates ...\n";
         return 2;
     }
     const std::string cmd = argv[1];
@@ -393,6 +417,7 @@ int main(int argc, char** argv) {
         if (cmd == "geom" && argc >= 4) { return cmdGeom(argv[2], argv[3]); }
         if (cmd == "invert" && argc >= 5) { return cmdInvert(argv[2], argv[3], argv[4]); }
         if (cmd == "topology" && argc >= 4) { return cmdTopology(argv[2], argv[3]); }
+        if (cmd == "rates" && argc >= 5) { return cmdRates(argv[2], argv[3], argv[4]); }
     } catch (const std::exception& e) {
         std::cerr << "ref_driver error: " << e.what() << '\n';
         return 1;

@@ -96,6 +96,7 @@ SIGNATURES = {
     "psim_model_run": (ctypes.c_int, [ctypes.c_void_p]),
     "psim_model_shape": (ctypes.c_int, [ctypes.c_void_p, _c_i64p, _c_i64p, _c_i64p, _c_i64p, _c_i64p]),
     "psim_model_measurements": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "psim_model_set_measurements": (ctypes.c_int, [ctypes.c_void_p, _c_dp, ctypes.c_int64]),
     "psim_model_series": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, _c_dp, _c_dp]),
     "psim_model_tallies": (ctypes.c_int, [ctypes.c_void_p, _c_i64p, _c_dp]),
     "psim_model_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RunCounters)]),
@@ -147,6 +148,7 @@ SIGNATURES = {
     "psim_mlp_predict": (ctypes.c_int, [ctypes.c_void_p, _c_fp, ctypes.c_int32, _c_fp]),
     "psim_mlp_destroy": (None, [ctypes.c_void_p]),
     "psim_geom_intersect": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_dp, _c_i32p]),
+    "psim_rates": (ctypes.c_int, [_c_dp, ctypes.c_int64, _c_dp, _c_dp, _c_i32p, ctypes.c_int, _c_dp]),
     "psim_geom_on_line": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_tri_contains": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
     "psim_geom_edge_index": (ctypes.c_int, [ctypes.c_int64, _c_dp, _c_dp, _c_i32p]),
@@ -271,6 +273,14 @@ class Model:
         out = np.zeros((self.n_sensors, 6))
         _check(lib().psim_model_measurements(self._h, _dp(out)))
         return out
+
+    def set_measurements(self, stats: np.ndarray) -> "Model":
+        """Replaces the per-run results with stats[runs, S, 6] made elsewhere (psim_model_set_measurements)."""
+        s = np.ascontiguousarray(stats, dtype=np.float64)
+        if s.ndim != 3 or s.shape[1:] != (self.n_sensors, 6):
+            raise ValueError(f"stats must be [runs, {self.n_sensors}, 6]")
+        _check(lib().psim_model_set_measurements(self._h, _dp(s), s.shape[0]))
+        return self
 
     def series(self, run: int = 0) -> Tuple[np.ndarray, np.ndarray]:
         temps = np.zeros((self.n_sensors, self.n_recorded))
@@ -528,6 +538,21 @@ def final_temps_noalloc(desc: InterpDesc, energy_dev: int, start_step: int, out_
 
 def final_temps_noalloc_max_bytes() -> int:
     return int(lib().psim_final_temps_noalloc_max_bytes())
+
+
+def rates(mat_params, T, freq, pol, precision=FP64) -> np.ndarray:
+    """Material::relaxRates as the FP32 or FP64 transport kernel evaluates it on the GPU:
+    [n, 3] normal, Umklapp and impurity rates (1/s) for the cases (T K, freq rad/s, pol 0/1)."""
+    mp = np.ascontiguousarray(mat_params, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    f = np.ascontiguousarray(freq, dtype=np.float64)
+    p = np.ascontiguousarray(pol, dtype=np.int32)
+    n = T.shape[0]
+    if mp.shape != (8,) or f.shape != (n,) or p.shape != (n,):
+        raise ValueError("mat_params needs 8 values and T, freq, pol one value per case")
+    out = np.zeros((n, 3))
+    _check(lib().psim_rates(_dp(mp), n, _dp(T), _dp(f), _i32(p), int(precision), _dp(out)))
+    return out
 
 
 def geom_intersect(a: np.ndarray, b: np.ndarray):

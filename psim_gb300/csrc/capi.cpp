@@ -168,6 +168,11 @@ int psim_model_shape(const psim_model* m, int64_t* n_sensors, int64_t* n_recorde
     return PSIM_OK;
 }
 
+int psim_model_set_measurements(psim_model* m, const double* stats, int64_t runs) {
+    if (m == nullptr || stats == nullptr || runs < 1) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
+    return guard([&]() { m->m->set_measurements(stats, static_cast<std::size_t>(runs)); });
+}
+
 int psim_model_measurements(const psim_model* m, double* stats) {
     if (m == nullptr || stats == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     if (m->m->measurements().empty()) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
@@ -612,6 +617,15 @@ int psim_geom_tri_contains(int64_t n, const double* tris, const double* pts, int
 int psim_geom_edge_index(int64_t n, const double* tris, const double* pts, int32_t* out) {
     if (n < 0 || (n > 0 && (tris == nullptr || pts == nullptr || out == nullptr))) { return fail(PSIM_ERR_INVALID, "bad arguments"); }
     return guard([&]() { psim::gpu::geom_edge_index(n, tris, pts, out); });
+}
+
+int psim_rates(const double* mat_params, int64_t n, const double* T, const double* freq, const int32_t* pol, int precision,
+               double* out) {
+    if (n < 0 || mat_params == nullptr || (n > 0 && (T == nullptr || freq == nullptr || pol == nullptr || out == nullptr))
+        || (precision != PSIM_PRECISION_FP32 && precision != PSIM_PRECISION_FP64)) {
+        return fail(PSIM_ERR_INVALID, "bad arguments");
+    }
+    return guard([&]() { psim::gpu::rates_probe(mat_params, n, T, freq, pol, precision, out); });
 }
 
 int psim_sampling_alias_table(const double* table, uint32_t* out) {

@@ -23,6 +23,8 @@ namespace psim::gpu {
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
 void launch_population_max(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters, cudaStream_t stream);
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
+void launch_rates32(const MaterialDev& m, const SensorDev* s, const float* w, const int* pol, int n, double* out, cudaStream_t stream);
+void launch_rates64(const MaterialDev& m, const double* T, const double* f, const int* pol, int n, double* out, cudaStream_t stream);
 int occupancy_f32(bool staged, int block, std::size_t smem);
 int occupancy_f64(std::size_t smem);
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
@@ -150,6 +152,69 @@ __global__ void unpack_kernel(const TallySlot* t, std::uint32_t S, std::uint64_t
 }// namespace
 
 std::vector<std::uint32_t> alias_table_of(const double* tab) { return alias_table(tab); }
+
+MaterialDev material_dev(const double* pr) {
+    MaterialDev md{};
+    md.b_l = pr[0];
+    md.b_tn = pr[1];
+    md.b_tu = pr[2];
+    md.b_i = pr[3];
+    md.w = pr[4];
+    md.width64 = pr[5];
+    md.w_max_la64 = pr[6];
+    md.w_max_ta64 = pr[7];
+    md.cL = static_cast<float>(pr[0] * 1e26);
+    md.cTN = static_cast<float>(pr[1] * 1e13);
+    md.cTU = static_cast<float>(pr[2] * 1e26);
+    md.cI = static_cast<float>(pr[3] * 1e52);
+    md.w_cut = static_cast<float>(pr[4] / 1e13);
+    md.width = static_cast<float>(pr[5] / 1e13);
+    md.w_max_la = static_cast<float>(pr[6] / 1e13);
+    md.w_max_ta = static_cast<float>(pr[7] / 1e13);
+    return md;
+}
+
+void sensor_rate_factors(double T, SensorDev& sd) {
+    constexpr double kHbar = 1.054517e-34;// psim/src/material.cpp:13-14
+    constexpr double kBoltz = 1.38065e-23;
+    sd.T = T;
+    sd.T3 = static_cast<float>(T * T * T);
+    sd.T4 = static_cast<float>(T * T * T * T);
+    sd.xk = static_cast<float>(kHbar * 1e13 / (kBoltz * T));
+}
+
+void rates_probe(const double* mat_params, std::int64_t n, const double* T, const double* f, const std::int32_t* pol,
+                 int precision, double* out) {
+    if (n <= 0) { return; }
+    if (n > (std::int64_t{ 1 } << 24)) { throw std::invalid_argument("at most 2^24 rate cases per call"); }
+    const MaterialDev m = material_dev(mat_params);
+    const auto cnt = static_cast<std::size_t>(n);
+    Buf pol_d;
+    Buf out_d;
+    pol_d.upload(std::vector<std::int32_t>(pol, pol + cnt));
+    out_d.alloc(cnt * 3 * sizeof(double));
+    if (precision == 0) {// the FP32 kernel's inputs: per-sensor factors of T, frequency in 1e13 rad/s
+        std::vector<SensorDev> s(cnt);
+        std::vector<float> w(cnt);
+        for (std::size_t i = 0; i < cnt; ++i) {
+            sensor_rate_factors(T[i], s[i]);
+            w[i] = static_cast<float>(f[i] / 1e13);
+        }
+        Buf s_d;
+        Buf w_d;
+        s_d.upload(s);
+        w_d.upload(w);
+        launch_rates32(m, s_d.as<SensorDev>(), w_d.as<float>(), pol_d.as<int>(), static_cast<int>(n), out_d.as<double>(), nullptr);
+    } else {
+        Buf t_d;
+        Buf f_d;
+        t_d.upload(std::vector<double>(T, T + cnt));
+        f_d.upload(std::vector<double>(f, f + cnt));
+        launch_rates64(m, t_d.as<double>(), f_d.as<double>(), pol_d.as<int>(), static_cast<int>(n), out_d.as<double>(), nullptr);
+    }
+    check(cudaGetLastError(), "rates kernel");
+    check(cudaMemcpy(out, out_d.p, cnt * 3 * sizeof(double), cudaMemcpyDeviceToHost), "rates copy");
+}
 
 // Device cell records from the flattened description: the FP32 cell-local form (outward
 // normals, offsets, edge links, neighbour entry edges) and the FP64 reference form.
@@ -383,24 +448,7 @@ Engine::Engine(const SimDesc& d)
     std::vector<float> centre32(static_cast<std::size_t>(d.n_materials) * kBins);
     std::vector<float> vel32(static_cast<std::size_t>(d.n_materials) * 2 * kBins);
     for (std::uint32_t m = 0; m < d.n_materials; ++m) {
-        const double* pr = &d.mat_params[8 * m];
-        MaterialDev& md = mats[m];
-        md.b_l = pr[0];
-        md.b_tn = pr[1];
-        md.b_tu = pr[2];
-        md.b_i = pr[3];
-        md.w = pr[4];
-        md.width64 = pr[5];
-        md.w_max_la64 = pr[6];
-        md.w_max_ta64 = pr[7];
-        md.cL = static_cast<float>(pr[0] * 1e26);
-        md.cTN = static_cast<float>(pr[1] * 1e13);
-        md.cTU = static_cast<float>(pr[2] * 1e26);
-        md.cI = static_cast<float>(pr[3] * 1e52);
-        md.w_cut = static_cast<float>(pr[4] / 1e13);
-        md.width = static_cast<float>(pr[5] / 1e13);
-        md.w_max_la = static_cast<float>(pr[6] / 1e13);
-        md.w_max_ta = static_cast<float>(pr[7] / 1e13);
+        mats[m] = material_dev(&d.mat_params[8 * m]);
         for (int b = 0; b < kBins; ++b) {
             centre32[m * kBins + b] = static_cast<float>(d.mat_freq[m * kBins + b] / 1e13);
             vel32[(m * 2) * kBins + b] = static_cast<float>(d.mat_vel[(m * 2) * kBins + b]);
@@ -423,15 +471,9 @@ Engine::Engine(const SimDesc& d)
 
     // ---- sensors
     std::vector<SensorDev> sens(d.n_sensors);
-    constexpr double kHbar = 1.054517e-34;
-    constexpr double kBoltz = 1.38065e-23;
     for (std::uint32_t s = 0; s < d.n_sensors; ++s) {
-        const double T = d.sensor_temp[s];
         SensorDev& sd = sens[s];
-        sd.T = T;
-        sd.T3 = static_cast<float>(T * T * T);
-        sd.T4 = static_cast<float>(T * T * T * T);
-        sd.xk = static_cast<float>(kHbar * 1e13 / (kBoltz * T));
+        sensor_rate_factors(d.sensor_temp[s], sd);
         sd.material = d.sensor_material[s];
         if (sd.material >= d.n_materials) { throw std::invalid_argument("sensor material out of range"); }
         sd.base_table = d.sensor_base_table[s];

@@ -194,6 +194,17 @@ void geom_on_line(std::int64_t n, const double* lines, const double* pts, std::i
 void geom_tri_contains(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
 void geom_edge_index(std::int64_t n, const double* tris, const double* pts, std::int32_t* out);
 
+// Device material record from (b_l, b_tn, b_tu, b_i, w, bin width, w_max LA, w_max TA), and a
+// sensor's FP32 rate factors of its temperature T (T^3, T^4, hbar 1e13 / (k T)).
+struct MaterialDev;
+struct SensorDev;
+MaterialDev material_dev(const double* params);
+void sensor_rate_factors(double T, SensorDev& sd);
+// Material::relaxRates on the GPU for n cases (T[i], f[i] rad/s, pol[i] 0 LA / 1 TA) of one
+// material: out[n][3] = N, U, I rates (1/s) from the FP32 (precision 0) or FP64 kernel's rates.
+void rates_probe(const double* mat_params, std::int64_t n, const double* T, const double* f, const std::int32_t* pol,
+                 int precision, double* out);
+
 // The Walker alias table the engine uploads for one cumulative table (tab[1000][2]): 2048 words.
 std::vector<std::uint32_t> alias_table_of(const double* tab);
 

@@ -109,9 +109,9 @@ __device__ __forceinline__ float3 rates32(const MaterialDev& m, const SensorDev&
         u = n;
     } else {
         n = (w < m.w_cut) ? m.cTN * w * s.T4 : 0.f;
-        if (w >= m.w_cut) {// sinh(x) = (e^x - e^-x) / 2 with x = hbar w / kT, here x > 0.1
-            const float ex = __expf(w * s.xk);
-            u = __fdividef(2.f * m.cTU * w2 * ex, ex * ex - 1.f);// cTU w^2 / sinh(x)
+        if (w >= m.w_cut) {// 1 / sinh(x) = 2 e^-x / (1 - e^-2x) with x = hbar w / kT > 0: no overflow at any T
+            const float em = __expf(-w * s.xk);
+            u = __fdividef(2.f * m.cTU * w2 * em, 1.f - em * em);// cTU w^2 / sinh(x)
         } else {
             u = 0.f;
         }
@@ -534,7 +534,21 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
     window_flush(P, g_smem);
 }
 
+// The FP32 rates on given inputs (a known-answer check against Material::relaxRates).
+__global__ void rates32_kernel(MaterialDev m, const SensorDev* s, const float* w, const int* pol, int n, double* out) {
+    const int i = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) { return; }
+    const float3 r = rates32(m, s[i], w[i], pol[i]);
+    out[3 * i] = r.x;
+    out[3 * i + 1] = r.y;
+    out[3 * i + 2] = r.z;
+}
+
 }// namespace
+
+void launch_rates32(const MaterialDev& m, const SensorDev* s, const float* w, const int* pol, int n, double* out, cudaStream_t stream) {
+    if (n > 0) { rates32_kernel<<<(n + 255) / 256, 256, 0, stream>>>(m, s, w, pol, n, out); }
+}
 
 // Largest population of the run (counters[3]) from the per-step populations.
 __global__ void population_max_kernel(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters) {

@@ -36,16 +36,34 @@ __device__ __forceinline__ double vel64(const StepParams& P, const Ph64& p) {
     return P.vel64[(smat_of(p.binw) * 2U + static_cast<std::uint32_t>(meta_pol(p.meta))) * kBins + bin_of(p.binw)];
 }
 
-// Material rates in FP64 (psim/src/material.cpp:207-239).
+// x^3 and x^4 rounded once, as a correctly rounded pow(x, 3.) / pow(x, 4.) returns them: the
+// products are carried exactly as unevaluated sums of two doubles (Dekker's product, with the
+// low part from an FMA) and rounded at the end.
+__device__ __forceinline__ double cube64(double x) {
+    const double s = x * x;
+    const double se = fma(x, x, -s);     // x^2 = s + se exactly
+    const double c = s * x;
+    const double ce = fma(s, x, -c);     // s x = c + ce exactly
+    return c + fma(se, x, ce);
+}
+__device__ __forceinline__ double quartic64(double x) {
+    const double s = x * x;
+    const double se = fma(x, x, -s);
+    const double q = s * s;
+    const double qe = fma(s, s, -q);     // s^2 = q + qe exactly
+    return q + fma(2. * s, se, qe);      // x^4 = q + qe + 2 s se + se^2 (se^2 is below the rounding)
+}
+
+// Material rates in FP64 (Material::relaxRates, psim/src/material.cpp:54-62,207-239).
 __device__ __forceinline__ void rates64(const MaterialDev& m, double T, double f, int pol, double r[3]) {
     if (pol == 0) {
-        r[0] = m.b_l * f * f * pow(T, 3.);
-        r[1] = m.b_l * f * f * pow(T, 3.);
+        r[0] = m.b_l * f * f * cube64(T);
+        r[1] = r[0];
     } else {
-        r[0] = (f < m.w) ? m.b_tn * f * pow(T, 4.) : 0.;
+        r[0] = (f < m.w) ? m.b_tn * f * quartic64(T) : 0.;
         r[1] = (f >= m.w) ? m.b_tu * f * f / sinh(kHbar64 * f / (T * kBoltz64)) : 0.;
     }
-    r[2] = m.b_i * pow(f, 4.);
+    r[2] = m.b_i * quartic64(f);
 }
 
 __device__ __forceinline__ void iso_dir(Ph64& p, Stream& rs) {
@@ -346,6 +364,21 @@ __global__ void __launch_bounds__(kBlock) step_kernel_f64(const StepParams P) {
 }
 
 }// namespace
+
+// The FP64 rates on given inputs (a known-answer check against Material::relaxRates).
+__global__ void rates64_kernel(MaterialDev m, const double* T, const double* f, const int* pol, int n, double* out) {
+    const int i = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x);
+    if (i >= n) { return; }
+    double r[3];
+    rates64(m, T[i], f[i], pol[i], r);
+    out[3 * i] = r[0];
+    out[3 * i + 1] = r[1];
+    out[3 * i + 2] = r[2];
+}
+
+void launch_rates64(const MaterialDev& m, const double* T, const double* f, const int* pol, int n, double* out, cudaStream_t stream) {
+    if (n > 0) { rates64_kernel<<<(n + 255) / 256, 256, 0, stream>>>(m, T, f, pol, n, out); }
+}
 
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream) {
     step_kernel_f64<<<grid, kBlock, smem, stream>>>(P);

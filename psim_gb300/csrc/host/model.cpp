@@ -611,6 +611,20 @@ std::vector<std::array<double, 6>> HostModel::averaged() const {// OutputManager
     return out;
 }
 
+// OutputManager::addMeasurement for every sensor of every run (psim/src/outputManager.cpp:116-118),
+// from statistics made elsewhere.
+void HostModel::set_measurements(const double* stats, std::size_t runs) {
+    const std::size_t S = sensors_.size();
+    std::vector<std::vector<Measurement>> r(runs, std::vector<Measurement>(S));
+    for (std::size_t k = 0; k < runs; ++k) {
+        for (std::size_t s = 0; s < S; ++s) {
+            r[k][s].id = s;
+            std::copy(stats + (k * S + s) * 6, stats + (k * S + s) * 6 + 6, r[k][s].stats.begin());
+        }
+    }
+    runs_ = std::move(r);
+}
+
 void HostModel::tallies(std::int64_t* energy, double* flux) const {
     if (!engine_) { throw std::runtime_error("the model has not been run"); }
     engine_->tallies(energy, flux, recorded_);
@@ -655,6 +669,11 @@ void HostModel::export_results(const std::string& json_path, double seconds) con
     }
     const std::size_t S = sensors_.size();
     const std::size_t K = recorded_;
+    for (const auto& r : runs_) {
+        for (const auto& m : r) {
+            if (m.temps.size() < K || m.fluxes.size() < 2 * K) { throw std::runtime_error("the runs carry no per-step series to export"); }
+        }
+    }
     std::vector<double> t(S * K, 0.);
     std::vector<double> f(S * K * 2, 0.);
     for (const auto& r : runs_) {

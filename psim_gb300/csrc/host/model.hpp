@@ -109,6 +109,8 @@ public:
     SimType type() const noexcept { return type_; }
     const std::vector<std::vector<Measurement>>& measurements() const noexcept { return runs_; }
     std::vector<std::array<double, 6>> averaged() const;
+    // Replaces the per-run results with given statistics stats[runs][S][6] (no per-step series).
+    void set_measurements(const double* stats, std::size_t runs);
     void tallies(std::int64_t* energy, double* flux) const;
     const gpu::RunCounters& counters() const;
     double last_seconds() const noexcept { return last_seconds_; }

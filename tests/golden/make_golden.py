@@ -3,7 +3,8 @@ sources (oracle/_ref/ref_driver, see oracle/ref_recipe/Makefile).  Run it where 
 reference tree is available:
 
     python tests/golden/make_golden.py --reference /path/to/reference [--skip-runs]
-        [--only geom,tables,invert,runs,topology,seeded,demos,headline,headline_tables,headline_topology]
+        [--only geom,tables,invert,runs,topology,seeded,demos,headline,headline_tables,headline_topology,rates,
+                exports]
         [--demo <demo>[,<demo>]]
 
 The demo runs dominate: each of the 16 runs of kinked_demo_120_35_spec (6174 cells, a 2e7
@@ -15,6 +16,8 @@ Outputs (all small):
                          Triangle normals, area and getRandPoint on random and degenerate cases
   tables_<model>.npz     material tables after Model::initializeMaterialTables
   invert_<model>.npz     SensorInterpreter results for given tallies
+  rates.npz              Material::relaxRates of two materials on a (T, frequency, polarization) grid
+  export_<model>.npz     a seeded run's per-run statistics and the ss_ table the reference wrote for it
   topology_<model>.npz   the assembled model (cells, sensors, edge sub-surfaces) of every model
                          file here, demos included
   runs_<model>.npz       per-sensor results of 16 seeded reference runs (statistical parity)
@@ -265,6 +268,64 @@ def make_tables(paths):
         print(f"tables_{name}.npz: {nt} temperatures, kept {keep}")
 
 
+# ---------------------------------------------------------------- the steady-state writer
+EXPORTS = (("bar_runs", 5), ("bar_ss", 6), ("si_ge_bar", 7))  # model, seed
+
+
+def make_exports(paths):
+    """export_<model>.npz: one seeded reference run's per-run statistics (as the run dump prints
+    them, 17 significant digits) and the ss_ table OutputManager::exportResults wrote for that run
+    (psim/src/outputManager.cpp:13-38,40-78): its header line and its body bytes."""
+    for name, seed in EXPORTS:
+        with tempfile.TemporaryDirectory() as td:
+            model = os.path.join(td, name + ".json")
+            with open(paths[name], "rb") as f, open(model, "wb") as g:
+                g.write(f.read())
+            dump = os.path.join(td, "d.json")
+            driver("run", model, dump, model, env=dict(os.environ, PSIM_SEED=str(seed)))
+            d = json.load(open(dump))
+            text = open(os.path.join(td, f"ss_{name}.txt"), "rb").read()
+        stats = np.array([[m["stats"] for m in run] for run in d["runs"]])
+        header, body = text.split(b"\n", 1)
+        np.savez_compressed(os.path.join(HERE, f"export_{name}.npz"), stats=stats, header=np.frombuffer(header, np.uint8),
+                            body=np.frombuffer(body, np.uint8))
+        print(f"export_{name}.npz: {stats.shape[0]} runs, {len(body)} body bytes")
+
+
+# ---------------------------------------------------------------- scattering rates
+def rate_cases():
+    """(T, frequency, polarization) known-answer grid for Material::relaxRates: temperatures from
+    2 K to 1000 K; frequencies on each material's bin centres (every 7th of the 1000) and both
+    sides of the TA cut-off w; both polarizations."""
+    temps = np.array([2.0, 5.0, 10.0, 20.0, 40.0, 50.0, 77.0, 150.0, 250.0, 280.0, 290.0, 300.0, 310.0, 320.0, 400.0,
+                      600.0, 1000.0])
+    return temps
+
+
+def make_rates(paths, name="si_ge_bar"):
+    """rates.npz: Material::relaxRates of the silicon and germanium of si_ge_bar on rate_cases(),
+    the cases of each material on its own frequency grid."""
+    model = json.load(open(paths[name]))
+    arrays = {}
+    with tempfile.TemporaryDirectory() as td:
+        for i, mat in enumerate(model["materials"]):
+            w_cut = mat["r_data"]["w"]
+            w_max = max(mat["d_data"]["max_freq_la"], mat["d_data"]["max_freq_ta"])
+            centres = (np.arange(1, 2000, 2) * (w_max / 1000.0) / 2.0)[::7]
+            freqs = np.concatenate([centres, [np.nextafter(w_cut, 0.0), w_cut, np.nextafter(w_cut, np.inf)]])
+            T, F, P = np.meshgrid(rate_cases(), freqs, [0.0, 1.0], indexing="ij")
+            cases = np.stack([T.ravel(), F.ravel(), P.ravel()], axis=1)
+            cp = os.path.join(td, "cases.bin")
+            op = os.path.join(td, "out.bin")
+            cases.astype("<f8").tofile(cp)
+            driver("rates", paths[name], cp, op)
+            out = np.fromfile(op, dtype="<f8").reshape(len(model["materials"]), len(cases), 3)
+            arrays[f"m{i}_cases"] = cases
+            arrays[f"m{i}_rates"] = out[i]
+    np.savez_compressed(os.path.join(HERE, "rates.npz"), **arrays)
+    print("rates.npz:", {k: v.shape for k, v in arrays.items()})
+
+
 # ---------------------------------------------------------------- model assembly
 def read_topology(path):
     """The reference's assembled model as written by `ref_driver topology`: per cell its sensor,
@@ -441,6 +502,10 @@ def main():
         make_runs(paths, list(model_specs()))
     if only is None or "headline_tables" in only:
         make_tables_two_materials(paths)
+    if only is None or "rates" in only:
+        make_rates(paths)
+    if only is None or "exports" in only:
+        make_exports(paths)
     if only is None or "headline_topology" in only:
         make_topology({k: paths[k] for k in headline_specs()})
     if not args.skip_runs and (only is None or "headline" in only):

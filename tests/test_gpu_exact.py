@@ -85,3 +85,52 @@ def test_inversion_bit_exact(api, name):
         for v in temps[s_, 1:]:
             acc += float(v)
         assert finals[s_] == acc / (temps.shape[1] - 1)
+
+
+def _ulps(a, b):
+    """Distance in units in the last place between positive doubles (or zeros) a and b."""
+    ia = np.asarray(a, dtype=np.float64).view(np.int64)
+    ib = np.asarray(b, dtype=np.float64).view(np.int64)
+    return np.abs(ia - ib)
+
+
+def test_rates_known_answers(api):
+    """Material::relaxRates (psim/src/material.cpp:54-62,207-239) as the transport kernels
+    evaluate it, against the reference's own values (tests/golden/rates.npz) for silicon and
+    germanium on a grid of temperatures (2-1000 K), frequencies (every 7th bin centre and both
+    sides of the TA cut-off w) and both polarizations.
+
+    FP64: the normal and impurity rates (products with T^3, T^4, f^4) are bit-exact with the
+    reference's correctly rounded pow; the TA Umklapp rate divides by sinh, which CUDA and the
+    host's libm each round within their stated bounds, so it is held to 4 units in the last place.
+    FP32: every rate's error, relative to the case's total rate (the quantity that sets the time
+    to the next scattering event and the branch probabilities), stays below 2e-6 from 20 K up and
+    below 2e-5 at any temperature of the grid.  The float frequency carries a relative error of
+    up to 6e-8, so the Umklapp factor e^-x (x = hbar w / kT) carries x times that: at 2 K x
+    reaches about 60 in germanium, where the Umklapp rate is the whole total."""
+    gold = np.load(os.path.join(GOLDEN, "rates.npz"))
+    m = api.Model(model_path("si_ge_bar"))
+    d = m.sim_desc()
+    params = np.ctypeslib.as_array(d.mat_params, shape=(2, 8)).copy()
+    for i, name in enumerate(("silicon", "germanium")):
+        cases = gold[f"m{i}_cases"]
+        ref = gold[f"m{i}_rates"]
+        T, f, pol = cases[:, 0], cases[:, 1], cases[:, 2].astype(np.int32)
+        r64 = api.rates(params[i], T, f, pol, api.FP64)
+        assert np.array_equal(r64 == 0.0, ref == 0.0)
+        exact_nu = np.array_equal(r64[:, 0], ref[:, 0]) and np.array_equal(r64[:, 2], ref[:, 2])
+        la = pol == 0
+        exact_u_la = np.array_equal(r64[la, 1], ref[la, 1])
+        u_ulps = _ulps(r64[~la, 1], ref[~la, 1])
+        print(f"{name} fp64: N and I bit-exact {exact_nu}, LA Umklapp bit-exact {exact_u_la}, TA Umklapp "
+              f"{(u_ulps == 0).mean():.1%} bit-exact, at most {u_ulps.max()} ulp")
+        assert exact_nu and exact_u_la
+        assert u_ulps.max() <= 4
+        r32 = api.rates(params[i], T, f, pol, api.FP32)
+        total = ref.sum(axis=1, keepdims=True)
+        rel = np.abs(r32 - ref) / total
+        print(f"{name} fp32: largest error {rel.max():.2e} of the total rate "
+              f"(T {T[rel.max(axis=1).argmax()]:g} K, f {f[rel.max(axis=1).argmax()]:.4g} rad/s)")
+        assert np.all(np.isfinite(r32))
+        assert rel.max() < 2e-5
+        assert rel[T >= 20.0].max() < 2e-6

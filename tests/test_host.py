@@ -391,3 +391,35 @@ def test_rate_inputs_are_refused_before_any_device_work(api, tmp_path):
             api.Simulator(d)
         assert e.value.code == api.PSIM_ERR_INVALID
     model.close()
+
+
+@pytest.mark.parametrize("name", ["bar_runs", "bar_ss", "si_ge_bar"])
+def test_steady_state_table_is_byte_identical_to_reference_writer(api, name, tmp_path):
+    """OutputManager::exportResults / calculateAverages / steadyStateExport
+    (psim/src/outputManager.cpp:13-38,40-78) against the table the reference itself wrote for
+    a seeded run (tests/golden/export_<name>.npz): fed the same per-run statistics, the writer
+    gives the same body, byte for byte, and the same header up to its date and time."""
+    import re
+    gold = np.load(os.path.join(GOLDEN, f"export_{name}.npz"))
+    src = model_path(name)
+    model_file = os.path.join(str(tmp_path), name + ".json")
+    with open(src, "rb") as f, open(model_file, "wb") as g:
+        g.write(f.read())
+    m = api.Model(model_file)
+    m.set_measurements(gold["stats"])
+    m.export(model_file, 0.0)
+    text = open(os.path.join(str(tmp_path), f"ss_{name}.txt"), "rb").read()
+    header, body = text.split(b"\n", 1)
+    assert body == gold["body"].tobytes()
+    date = rb"\d{4}-\d\d-\d\d \d\d:\d\d:\d\d"
+    assert re.sub(date, b"DATE", header) == re.sub(date, b"DATE", gold["header"].tobytes())
+    # the averaged statistics behind the table are the reference's calculateAverages
+    assert np.allclose(m.measurements(), gold["stats"].mean(axis=0), rtol=1e-15, atol=0)
+
+
+def test_periodic_export_needs_per_step_series(api, tmp_path):
+    """Statistics set from elsewhere carry no per-step series: a periodic table of them is refused."""
+    m = api.Model(model_path("bar_periodic"))
+    m.set_measurements(np.zeros((1, m.n_sensors, 6)))
+    with pytest.raises(Exception, match="per-step series"):
+        m.export(os.path.join(str(tmp_path), "p.json"), 0.0)
