@@ -265,6 +265,9 @@ struct StepParams {
     // 'step', then the newborns of each covered step j at [new_begin[j], new_begin[j+1]) after
     // them, with ids from id_base_f[j] and birth groups [group_begin_f[j], group_begin_f[j+1]).
     std::uint32_t n_fused;
+    // Plain step boundaries (no edge impact and no scattering before the boundary) are crossed in
+    // a warp-uniform loop while at least this many lanes of the warp can cross one (0: never)
+    std::uint32_t coast_lanes;
     std::uint32_t new_begin[kMaxFused + 1];
     std::uint32_t id_base_f[kMaxFused];
     std::uint32_t group_begin_f[kMaxFused + 1];

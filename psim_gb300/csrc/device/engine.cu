@@ -25,7 +25,7 @@ void launch_population_max(const std::uint32_t* population, std::uint32_t n, uns
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
 void launch_rates32(const MaterialDev& m, const SensorDev* s, const float* w, const int* pol, int n, double* out, cudaStream_t stream);
 void launch_rates64(const MaterialDev& m, const double* T, const double* f, const int* pol, int n, double* out, cudaStream_t stream);
-int occupancy_f32(bool staged, int block, std::size_t smem);
+int occupancy_f32(unsigned stage_mask, int block, std::size_t smem);
 int occupancy_f64(std::size_t smem);
 void interpret_device(const InterpDesc& d, const long long* energy, const double* flux, double* temps_h, double* fluxes_h,
                       double* stats_h, cudaStream_t stream, InterpCache* cache);
@@ -724,6 +724,8 @@ void Engine::run(int precision, void* stream_ptr) {
         fuse_cap = std::min<std::uint32_t>(kMaxFused, static_cast<std::uint32_t>(std::atoi(f)));
     }
     std::uint32_t fused = 1;
+    P.coast_lanes = coast_lanes_;
+    if (const char* c = std::getenv("PSIM_GB300_COAST"); c != nullptr) { P.coast_lanes = static_cast<std::uint32_t>(std::max(0, std::atoi(c))); }
     std::size_t tally_b = tally_smem_bytes(d.n_sensors, 1);
     P.n_cells = d.n_cells;
     P.n_tables = d.n_tables;
@@ -734,7 +736,11 @@ void Engine::run(int precision, void* stream_ptr) {
     std::size_t smem = tally_b;
     int block = 256;
     bool stage = stage_tables_;
-    if (const char* st = std::getenv("PSIM_GB300_STAGE"); st != nullptr && std::atoi(st) == 0) { stage = false; }
+    bool tables_only = false;// stage the tables but not the cell records even where both fit
+    if (const char* st = std::getenv("PSIM_GB300_STAGE"); st != nullptr) {
+        stage = stage && std::atoi(st) != 0;
+        tables_only = std::atoi(st) == 2;
+    }
     if (!fp64 && stage) {
         int dev = 0;
         int optin = 0;
@@ -748,19 +754,24 @@ void Engine::run(int precision, void* stream_ptr) {
         const std::size_t sens_b = static_cast<std::size_t>(d.n_sensors) * sizeof(SensorDev);
         const std::size_t mat_b = static_cast<std::size_t>(d.n_materials) * sizeof(MaterialDev);
         const std::size_t emit_b = static_cast<std::size_t>(d.n_emitters) * sizeof(EmitterDev);
-        const std::size_t used = cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b;
-        if (used + tally_b <= budget) {// everything or nothing: the staged kernel reads every table from shared memory
+        const std::size_t tables_b = alias_b + vel_b + centre_b + sens_b + mat_b + emit_b;
+        // Everything when it fits next to the tally, else the tables without the cell records
+        // (large models: cells and, above kSharedSensors sensors, tallies in global memory).
+        const bool all = !tables_only && cells_b + tables_b + tally_b <= budget;
+        if (all || tables_b + tally_b <= budget) {
+            const std::size_t cb = all ? cells_b : 0;
+            const std::size_t used = cb + tables_b;
             while (fused < fuse_cap && used + tally_smem_bytes(d.n_sensors, fused + 1) <= budget) { ++fused; }
             tally_b = tally_smem_bytes(d.n_sensors, fused);
             P.off_cells = 0U;
-            P.off_alias = static_cast<std::uint32_t>(cells_b);
-            P.off_vel = static_cast<std::uint32_t>(cells_b + alias_b);
-            P.off_centre = static_cast<std::uint32_t>(cells_b + alias_b + vel_b);
-            P.off_sensors = static_cast<std::uint32_t>(cells_b + alias_b + vel_b + centre_b);
+            P.off_alias = static_cast<std::uint32_t>(cb);
+            P.off_vel = static_cast<std::uint32_t>(cb + alias_b);
+            P.off_centre = static_cast<std::uint32_t>(cb + alias_b + vel_b);
+            P.off_sensors = static_cast<std::uint32_t>(cb + alias_b + vel_b + centre_b);
             P.off_materials = static_cast<std::uint32_t>(P.off_sensors + sens_b);
             P.off_emitters = static_cast<std::uint32_t>(P.off_materials + mat_b);
             P.off_tally = static_cast<std::uint32_t>(used);
-            P.stage_mask = 7U;
+            P.stage_mask = all ? 7U : 6U;
             smem = used + tally_b;
             block = 1024;
         }
@@ -773,13 +784,13 @@ void Engine::run(int precision, void* stream_ptr) {
         smem = tally_b;
     };
     if (!fp64 && P.stage_mask == 0U) { unstaged_fuse(); }
-    int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(P.stage_mask != 0U, block, smem);
+    int occ = fp64 ? occupancy_f64(smem) : occupancy_f32(P.stage_mask, block, smem);
     if (occ <= 0 && !fp64 && P.stage_mask != 0U) {// cannot launch staged: fall back to global tables
         P.stage_mask = 0U;
         P.off_tally = 0U;
         block = 256;
         unstaged_fuse();
-        occ = occupancy_f32(false, block, smem);
+        occ = occupancy_f32(0U, block, smem);
     }
     if (fp64) { fused = 1; }
     occ = std::max(1, occ);

@@ -99,6 +99,9 @@ public:
     void set_grid(int blocks) { grid_override_ = blocks; }
     // Stage cells and tables into shared memory in the FP32 kernel when they fit (default on).
     void set_stage_tables(bool on) { stage_tables_ = on; }
+    // FP32 kernel: plain step boundaries are crossed in a warp-uniform loop while at least this
+    // many of a warp's 32 lanes cross one (0: every boundary takes the general segment).
+    void set_coast_lanes(std::uint32_t lanes) { coast_lanes_ = lanes > 32U ? 32U : lanes; }
     std::uint32_t last_stage_mask() const noexcept { return last_stage_mask_; }
     // Measurement steps per FP32 launch in the last run (1 for FP64).
     std::uint32_t last_fused() const noexcept { return last_fused_; }
@@ -136,6 +139,7 @@ private:
     std::uint64_t model_bytes_{ 0 };
     bool use_graph_{ true };
     bool stage_tables_{ true };
+    std::uint32_t coast_lanes_{ 0 };
     std::uint32_t last_stage_mask_{ 0 };
     std::uint32_t last_fused_{ 1 };
     bool stop_on_{ false };

@@ -23,52 +23,56 @@ namespace {
 
 extern __shared__ __align__(16) unsigned char g_smem[];
 
-// Read-only tables: the shared-memory copies in the staged kernel (kStaged), else global memory.
-// Compiled as two kernels so each reads its tables with direct shared or global loads.
-template<bool kStaged> __device__ __forceinline__ const CellF32* cells_of(const StepParams& P) {
-    if constexpr (kStaged) {
+// Read-only tables: the shared-memory copies where the kernel's staging mask M says so, else
+// global memory.  M is a compile-time copy of StepParams::stage_mask: bit 0 cell records, bits 1-2
+// the alias tables with the velocity and bin-centre tables (with them the sensor, material and
+// emitter records).  Each variant reads its tables with direct shared or global loads.
+constexpr unsigned kStageCells = 1U;
+constexpr unsigned kStageTables = 6U;
+template<unsigned M> __device__ __forceinline__ const CellF32* cells_of(const StepParams& P) {
+    if constexpr ((M & kStageCells) != 0U) {
         return reinterpret_cast<const CellF32*>(g_smem + P.off_cells);
     } else {
         return P.cells32;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const std::uint32_t* alias_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const std::uint32_t* alias_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const std::uint32_t*>(g_smem + P.off_alias);
     } else {
         return P.alias;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const float* vel_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const float* vel_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const float*>(g_smem + P.off_vel);
     } else {
         return P.vel32;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const SensorDev* sensors_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const SensorDev* sensors_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const SensorDev*>(g_smem + P.off_sensors);
     } else {
         return P.sensors;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const MaterialDev* materials_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const MaterialDev* materials_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const MaterialDev*>(g_smem + P.off_materials);
     } else {
         return P.materials;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const EmitterDev* emitters_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const EmitterDev* emitters_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const EmitterDev*>(g_smem + P.off_emitters);
     } else {
         return P.emitters;
     }
 }
-template<bool kStaged> __device__ __forceinline__ const float* centre_of(const StepParams& P) {
-    if constexpr (kStaged) {
+template<unsigned M> __device__ __forceinline__ const float* centre_of(const StepParams& P) {
+    if constexpr ((M & kStageTables) != 0U) {
         return reinterpret_cast<const float*>(g_smem + P.off_centre);
     } else {
         return P.centre32;
@@ -83,13 +87,13 @@ struct Ph32 {
 };
 
 // Group velocity of the phonon's bin (Material::getVel, psim/src/material.cpp:82-84).
-template<bool S> __device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
+template<unsigned S> __device__ __forceinline__ float vel32(const StepParams& P, std::uint32_t binw, int pol, bool phasor) {
     return phasor ? 1000.f : vel_of<S>(P)[(smat_of(binw) * 2U + static_cast<std::uint32_t>(pol)) * kBins + bin_of(binw)];
 }
 
 // Frequency in units of 1e13 rad/s (Material::getFreq, psim/src/material.cpp:77-80): bin
 // centre plus the stored uniform offset inside the bin in a deviational simulation.
-template<bool S> __device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
+template<unsigned S> __device__ __forceinline__ float omega32(const StepParams& P, std::uint32_t binw, bool phasor) {
     if (phasor) { return 1e-13f; }
     const std::uint32_t sm = smat_of(binw);
     const float c = centre_of<S>(P)[sm * kBins + bin_of(binw)];
@@ -148,7 +152,7 @@ __device__ __forceinline__ void reflect(Ph32& p, Stream& rs, float spec, float4 
 
 // Material::freqIndex + getFreq (psim/src/material.cpp:64-80) from an alias table of the
 // material 'mat'.
-template<bool S> __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
+template<unsigned S> __device__ __forceinline__ void sample_freq(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t table,
                                             std::uint32_t mat) {
     const std::uint32_t o = alias_draw(alias_of<S>(P) + static_cast<std::size_t>(table) * kAliasCols, rs.next());
     const std::uint32_t jit = P.full_sim ? 0U : (rs.next() >> 14);
@@ -158,7 +162,7 @@ template<bool S> __device__ __forceinline__ void sample_freq(const StepParams& P
 
 // Create newborn j of the launch's step jf (CellOriginBuilder / SurfaceOriginBuilder /
 // PhasorBuilder, psim/src/phononBuilder.cpp:6-49).  Returns the time left until the step boundary.
-template<bool S> __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t jf,
+template<unsigned S> __device__ __forceinline__ float spawn32(const StepParams& P, Ph32& p, Stream& rs, std::uint32_t jf,
                                                           std::uint32_t j) {
     const BirthGroup g = P.groups[find_group(P, P.group_begin_f[jf], P.group_begin_f[jf + 1], j)];
     p.id = P.id_base_f[jf] + j;
@@ -240,7 +244,7 @@ __device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, st
     L.events = 0;
 }
 
-template<bool S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive) {
+template<unsigned S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive) {
     if (i < n_alive) {
         const float4* in_pd = static_cast<const float4*>(P.in);
         const float4 a = in_pd[i];
@@ -282,6 +286,16 @@ __device__ __forceinline__ void next_exit(const CellF32* C, const Ph32& p, float
     }
 }
 
+// The lane's phonon enters 'step' at its start without computing random words ahead (a
+// coasting lane crosses boundaries at its own pace; the words are made where it next draws).
+__device__ __forceinline__ void lane_enter_step_lazy(const StepParams& P, Lane& L, std::uint32_t step) {
+    L.rs.init(P.key0, P.key1, step, L.p.id);
+    L.rem = P.dt;
+    L.need_target = true;
+    L.rates_ok = false;
+    L.events = 0;
+}
+
 // The phonon has reached its step's boundary: the outcome (alive into the next step or not,
 // tallied or not).  Returns true (the step is over).
 __device__ __forceinline__ bool boundary_outcome(const StepParams& P, const Lane& L, Outcome& out) {
@@ -300,12 +314,47 @@ __device__ __forceinline__ bool boundary_outcome(const StepParams& P, const Lane
     return true;
 }
 
+// One plain step boundary, if the phonon's next segment is one: its current event ends at the
+// step boundary (no scattering first) and its straight path meets no edge before it.  Then the
+// phonon drifts to the boundary exactly as segment32 would move it, and the outcome is the
+// boundary's; returns false (state unchanged but for the event set-up segment32 would do
+// first) when the next segment holds an impact, a scattering event or a new scattering time.
+template<unsigned S> __device__ __forceinline__ bool coast32(const StepParams& P, Lane& L, Outcome& out) {
+    Ph32& p = L.p;
+    if (L.need_target) {
+        if (p.tts <= 0.f || L.events + 1U > kMaxEventsPerStep) { return false; }
+        ++L.events;
+        L.target = (L.rem <= p.tts) ? L.rem : p.tts;
+        L.drifted = 0.f;
+        L.ncoll = 0;
+        L.changed = false;
+        L.need_target = false;
+    }
+    if (L.target != L.rem) { return false; }
+    const CellF32* C = cells_of<S>(P) + meta_cell(p.meta);
+    const float wx = p.dx * L.v;
+    const float wy = p.dy * L.v;
+    float tbest;
+    int ebest;
+    next_exit(C, p, wx, wy, meta_edge(p.meta), tbest, ebest);
+    const float left = L.target - L.drifted;
+    if (!(ebest < 0 || tbest > left)) { return false; }
+    p.px += wx * left;
+    p.py += wy * left;
+    L.drifted = L.target;
+    const float used = L.target;
+    L.rem -= used;
+    p.tts -= used;
+    L.need_target = true;
+    return boundary_outcome(P, L, out);
+}
+
 // One segment of a phonon's step: the straight flight to the next edge impact or to the end of
 // the current event (ModelSimulator::simulatePhonon / handleImpacts / nextImpact,
 // psim/src/modelSimulator.cpp:87-225).  Returns true when the phonon's step is over (it
 // reached the step boundary or was absorbed); the outcome says which.
 // The rare event-limit and collision-limit hits go straight to their global counters.
-template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out) {
+template<unsigned S> __device__ __forceinline__ bool segment32(const StepParams& P, Lane& L, Outcome& out) {
     Ph32& p = L.p;
     Stream& rs = L.rs;
     const bool phasor = meta_phasor(p.meta);
@@ -438,16 +487,16 @@ template<bool S> __device__ __forceinline__ bool segment32(const StepParams& P, 
 // lane; one that leaves the launch (or dies) frees the lane for the next work item.  The warp
 // stays full until the launch's work runs out instead of waiting for its slowest phonon.
 // P is a __grid_constant__ so the per-step arrays in it are read in place with a runtime index.
-template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const __grid_constant__ StepParams P) {
+template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const __grid_constant__ StepParams P) {
     __shared__ std::uint64_t stage_bar;
-    if constexpr (S) {// TMA bulk copies of the read-only tables into shared memory
+    if constexpr (S != 0U) {// TMA bulk copies of the read-only tables into shared memory
         if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
         __syncthreads();
         if (threadIdx.x == 0) {
-            const unsigned cells_b = (P.stage_mask & 1U) ? P.n_cells * static_cast<unsigned>(sizeof(CellF32)) : 0U;
-            const unsigned alias_b = (P.stage_mask & 2U) ? P.n_tables * kAliasCols * 4U : 0U;
-            const unsigned vel_b = (P.stage_mask & 4U) ? P.n_materials * 2U * kBins * 4U : 0U;
-            const unsigned centre_b = (P.stage_mask & 4U) ? P.n_materials * kBins * 4U : 0U;
+            const unsigned cells_b = (S & kStageCells) ? P.n_cells * static_cast<unsigned>(sizeof(CellF32)) : 0U;
+            const unsigned alias_b = P.n_tables * kAliasCols * 4U;
+            const unsigned vel_b = P.n_materials * 2U * kBins * 4U;
+            const unsigned centre_b = P.n_materials * kBins * 4U;
             const unsigned sens_b = P.n_sensors * static_cast<unsigned>(sizeof(SensorDev));
             const unsigned mat_b = P.n_materials * static_cast<unsigned>(sizeof(MaterialDev));
             const unsigned emit_b = P.n_emitters * static_cast<unsigned>(sizeof(EmitterDev));
@@ -456,16 +505,14 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
             bulk_to_shared(g_smem + P.off_materials, P.materials, mat_b, &stage_bar);
             if (emit_b != 0U) { bulk_to_shared(g_smem + P.off_emitters, P.emitters, emit_b, &stage_bar); }
             if (cells_b != 0U) { bulk_to_shared(g_smem + P.off_cells, P.cells32, cells_b, &stage_bar); }
-            if (alias_b != 0U) { bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, &stage_bar); }
-            if (vel_b != 0U) {
-                bulk_to_shared(g_smem + P.off_vel, P.vel32, vel_b, &stage_bar);
-                bulk_to_shared(g_smem + P.off_centre, P.centre32, centre_b, &stage_bar);
-            }
+            bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, &stage_bar);
+            bulk_to_shared(g_smem + P.off_vel, P.vel32, vel_b, &stage_bar);
+            bulk_to_shared(g_smem + P.off_centre, P.centre32, centre_b, &stage_bar);
         }
     }
     BlockTally bt;
     tally_init(P, bt, g_smem, P.n_fused);
-    if constexpr (S) {
+    if constexpr (S != 0U) {
         const bool ok = mbar_wait_bounded(&stage_bar);
         if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
             if (threadIdx.x == 0) { atomicAdd(P.counters + 5, 1ULL); }
@@ -512,7 +559,38 @@ template<bool S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(cons
         if (__ballot_sync(full, active) == 0U) { break; }
         Outcome o{ false, false, false, false, 0U, 0, 0 };
         bool done = false;
-        if (active) { done = segment32<S>(P, L, o); }
+        // Plain boundaries first, in a loop the warp runs while enough of its lanes cross one: a
+        // phonon on its way into the launch's next step stays here, so the segment below is
+        // mostly the phonon's next event (an impact, a scattering event, a new scattering time).
+        if (P.coast_lanes != 0U) {
+            bool coasting = active;
+            while (true) {
+                Outcome c{ false, false, false, false, 0U, 0, 0 };
+                const bool crossed = coasting && coast32<S>(P, L, c);
+                if (static_cast<std::uint32_t>(__popc(__ballot_sync(full, crossed))) < P.coast_lanes) {
+                    if (crossed) {// the warp stops here: this boundary goes to the common path below
+                        o = c;
+                        done = true;
+                    }
+                    break;
+                }
+                if (!crossed) {
+                    coasting = false;
+                } else if (c.alive && c.cont) {
+                    steps += 1U;
+                    window_add(P, g_smem, true, c.tallied, L.step() - P.step, c.sensor, meta_sign(L.p.meta), c.fx, c.fy);
+                    lane_enter_step_lazy(P, L, L.step() + 1U);
+                } else {// the launch's last boundary or the run's end: the common path below finishes it
+                    o = c;
+                    done = true;
+                    coasting = false;
+                }
+            }
+        }
+        if (active && !done) {
+            if (L.rs.left == 0) { L.rs.prefill(); }// most segments here draw: make the words together
+            done = segment32<S>(P, L, o);
+        }
         const bool finishing = active && done;
         const bool crossing = finishing && o.alive;// into step L.step + 1
         const bool stays = crossing && o.cont;
@@ -563,11 +641,20 @@ void launch_population_max(const std::uint32_t* population, std::uint32_t n, uns
     population_max_kernel<<<1, 1024, 0, stream>>>(population, n, counters);
 }
 
+// The kernel variant of a staging mask (0, tables only, or everything).
+const void* step_f32_fn(unsigned stage_mask) {
+    if (stage_mask == (kStageCells | kStageTables)) { return reinterpret_cast<const void*>(step_kernel_f32<kStageCells | kStageTables>); }
+    if (stage_mask == kStageTables) { return reinterpret_cast<const void*>(step_kernel_f32<kStageTables>); }
+    return reinterpret_cast<const void*>(step_kernel_f32<0U>);
+}
+
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
-    if (P.stage_mask != 0U) {
-        step_kernel_f32<true><<<grid, block, smem, stream>>>(P);
+    if (P.stage_mask == (kStageCells | kStageTables)) {
+        step_kernel_f32<kStageCells | kStageTables><<<grid, block, smem, stream>>>(P);
+    } else if (P.stage_mask == kStageTables) {
+        step_kernel_f32<kStageTables><<<grid, block, smem, stream>>>(P);
     } else {
-        step_kernel_f32<false><<<grid, block, smem, stream>>>(P);
+        step_kernel_f32<0U><<<grid, block, smem, stream>>>(P);
     }
 }
 
@@ -575,8 +662,8 @@ void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem,
 // dynamic shared-memory limit is a process-wide attribute: it is always raised to the device's
 // maximum (the same value for every caller), never to one model's need, so engines that run
 // side by side on other threads cannot lower it under each other's launches.
-int occupancy_f32(bool staged, int block, std::size_t smem) {
-    const void* fn = staged ? reinterpret_cast<const void*>(step_kernel_f32<true>) : reinterpret_cast<const void*>(step_kernel_f32<false>);
+int occupancy_f32(unsigned stage_mask, int block, std::size_t smem) {
+    const void* fn = step_f32_fn(stage_mask);
     int dev = 0;
     int optin = 0;
     cudaFuncAttributes fa{};

@@ -109,7 +109,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar) {
 // The tally of an FP32 launch (one slot per covered step), rebuilt from the parameters where it
 // is used so that no pointer to it stays live in registers.
 __device__ __forceinline__ BlockTally window_tally(const StepParams& P, unsigned char* smem) {
-    return BlockTally{ smem + P.off_tally, P.n_fused * P.n_sensors, P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors) };
+    const bool shared = P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors);
+    return BlockTally{ smem + P.off_tally, shared ? P.n_fused * P.n_sensors : 0U, shared };
 }
 
 // FP32 launch over several steps: a phonon ending step P.step + j at its boundary.  'crossing'
@@ -130,8 +131,8 @@ __device__ __forceinline__ void window_add(const StepParams& P, unsigned char* s
             atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx() + i), static_cast<unsigned long long>(fx));
             atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy() + i), static_cast<unsigned long long>(fy));
         }
-    } else {
-        atomicAdd(P.population + P.step + j + 1U, 1U);
+    } else {// tallies straight to global memory; the crossings are still counted per block
+        atomicAdd(bt.cross() + j, 1U);
         if (tallied) {
             TallySlot* t = P.tally + static_cast<std::size_t>(P.step + j + 1U - P.step_adj) * P.n_sensors + sensor;
             atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(sign)));
@@ -145,9 +146,8 @@ __device__ __forceinline__ void window_add(const StepParams& P, unsigned char* s
 // counts to the population of the steps they enter.
 __device__ __forceinline__ void window_flush(const StepParams& P, unsigned char* smem) {
     const BlockTally bt = window_tally(P, smem);
-    if (!bt.shared) { return; }
     __syncthreads();
-    const std::uint32_t n = P.n_fused * P.n_sensors;
+    const std::uint32_t n = bt.shared ? P.n_fused * P.n_sensors : 0U;
     for (std::uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         const std::uint32_t j = i / P.n_sensors;
         const std::uint32_t s = i - j * P.n_sensors;
@@ -185,27 +185,26 @@ __device__ __forceinline__ void tally_flush(const StepParams& P, BlockTally& bt,
 }
 
 __device__ __forceinline__ void tally_init(const StepParams& P, BlockTally& bt, unsigned char* smem, std::uint32_t slots) {
-    // layout: fx[slots*S], fy[slots*S] (8-byte aligned), count[slots*S], cross[kMaxFused];
-    // S <= kSharedSensors
+    // layout: fx[slots*S], fy[slots*S] (8-byte aligned), count[slots*S], cross[kMaxFused] with
+    // S <= kSharedSensors; cross[kMaxFused] alone for larger S (tallies in global memory)
     bt.shared = P.n_sensors <= static_cast<std::uint32_t>(kSharedSensors);
-    const std::uint32_t n = slots * P.n_sensors;
+    const std::uint32_t n = bt.shared ? slots * P.n_sensors : 0U;
     bt.base = smem + P.off_tally;
     bt.n = n;
-    if (bt.shared) {
-        for (std::uint32_t s = threadIdx.x; s < n; s += blockDim.x) {
-            bt.fx()[s] = 0;
-            bt.fy()[s] = 0;
-            bt.count()[s] = 0;
-        }
-        if (threadIdx.x < kMaxFused) { bt.cross()[threadIdx.x] = 0U; }
+    for (std::uint32_t s = threadIdx.x; s < n; s += blockDim.x) {
+        bt.fx()[s] = 0;
+        bt.fy()[s] = 0;
+        bt.count()[s] = 0;
     }
+    if (threadIdx.x < kMaxFused) { bt.cross()[threadIdx.x] = 0U; }
     __syncthreads();
 }
 
-// Shared bytes of a block's tally with 'slots' boundary slots of S sensors (0 when S exceeds
-// kSharedSensors: the tallies then go straight to global memory), 16-aligned.
+// Shared bytes of a block's tally with 'slots' boundary slots of S sensors, 16-aligned.  Above
+// kSharedSensors sensors the tallies go straight to global memory and only the per-boundary
+// crossing counts stay in shared memory.
 inline std::size_t tally_smem_bytes(std::uint32_t S, std::uint32_t slots = 1) {
-    if (S > static_cast<std::uint32_t>(kSharedSensors)) { return 0; }
+    if (S > static_cast<std::uint32_t>(kSharedSensors)) { return kMaxFused * 4; }
     return ((static_cast<std::size_t>(S) * slots * 20 + kMaxFused * 4 + 15) / 16) * 16;
 }
 

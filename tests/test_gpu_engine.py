@@ -55,16 +55,24 @@ def test_launch_shape_does_not_change_results(api, monkeypatch):
     assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
 
 
-@pytest.mark.parametrize("name", ["kinked_small", "plate_small", "bar_ss"])
-def test_steps_per_launch_do_not_change_results(api, monkeypatch, name):
+@pytest.mark.parametrize("name", ["kinked_small", "plate_small", "bar_ss", "plate_2560"])
+def test_steps_per_launch_do_not_change_results(api, monkeypatch, tmp_path, name):
     """An FP32 launch covers up to 16 measurement steps and carries phonons across the inner
-    boundaries in registers.  Tallies, the population history and the phonon-step count equal
-    those of one step per launch, with shared-memory tables and with global ones."""
+    boundaries in registers; plain boundaries are crossed in a warp-uniform loop while enough
+    lanes cross one.  Tallies, the population history and the phonon-step count equal those of
+    one step per launch, with every table in shared memory, with the tables but not the cell
+    records there, and with global ones, and whatever the coasting threshold.  plate_2560 has
+    more sensors than the shared-memory tally holds (tallies in global memory)."""
+    from psim_gb300 import modelgen as mg
+    path = (mg.write(mg.plate(nx=64, ny=40, num_phonons=30000, num_measurements=120, sim_time=0.12),
+                     os.path.join(str(tmp_path), "plate_2560.json")) if name == "plate_2560" else model_path(name))
     ref = None
-    for stage, fuse in (("1", "1"), ("1", "3"), ("1", "8"), ("1", "16"), ("0", "5")):
+    for stage, fuse, coast in (("1", "1", "0"), ("1", "3", "16"), ("1", "8", "1"), ("1", "16", "32"), ("0", "5", "16"),
+                               ("2", "7", "16"), ("2", "2", "0")):
         monkeypatch.setenv("PSIM_GB300_STAGE", stage)
         monkeypatch.setenv("PSIM_GB300_FUSE", fuse)
-        m = api.Model(model_path(name))
+        monkeypatch.setenv("PSIM_GB300_COAST", coast)
+        m = api.Model(path)
         m.run(seed=11)
         e, f = m.tallies()
         c = m.counters()
@@ -79,6 +87,7 @@ def test_steps_per_launch_do_not_change_results(api, monkeypatch, name):
         assert ref[3:] == got[3:], (stage, fuse)
     monkeypatch.delenv("PSIM_GB300_STAGE")
     monkeypatch.delenv("PSIM_GB300_FUSE")
+    monkeypatch.delenv("PSIM_GB300_COAST")
 
 
 def test_counters_and_phonon_steps(api):

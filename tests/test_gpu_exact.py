@@ -107,7 +107,10 @@ def test_rates_known_answers(api):
     to the next scattering event and the branch probabilities), stays below 2e-6 from 20 K up and
     below 2e-5 at any temperature of the grid.  The float frequency carries a relative error of
     up to 6e-8, so the Umklapp factor e^-x (x = hbar w / kT) carries x times that: at 2 K x
-    reaches about 60 in germanium, where the Umklapp rate is the whole total."""
+    reaches about 60 in germanium, where the Umklapp rate is the whole total.  Frequencies that
+    round to the same float as the TA cut-off w are left out of the FP32 comparison: there the
+    float comparison with w can take the other branch (Umklapp instead of normal scattering),
+    a choice the FP64 kernel makes exactly."""
     gold = np.load(os.path.join(GOLDEN, "rates.npz"))
     m = api.Model(model_path("si_ge_bar"))
     d = m.sim_desc()
@@ -129,6 +132,10 @@ def test_rates_known_answers(api):
         r32 = api.rates(params[i], T, f, pol, api.FP32)
         total = ref.sum(axis=1, keepdims=True)
         rel = np.abs(r32 - ref) / total
+        at_cut = (np.float32(f / 1e13) == np.float32(params[i][4] / 1e13)) & (f != params[i][4])
+        print(f"{name} fp32: {int(at_cut.sum())} cases within float rounding of the cut-off left out")
+        rel = rel[~at_cut]
+        T, f = T[~at_cut], f[~at_cut]
         print(f"{name} fp32: largest error {rel.max():.2e} of the total rate "
               f"(T {T[rel.max(axis=1).argmax()]:g} K, f {f[rel.max(axis=1).argmax()]:.4g} rad/s)")
         assert np.all(np.isfinite(r32))
