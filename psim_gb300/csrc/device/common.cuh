@@ -303,4 +303,18 @@ struct StepParams {
                                       // [6] backscatters at interfaces between materials
 };
 
+// One launch of the batched FP32 kernel: the same window of measurement steps for every model of
+// a batch.  params[m] is model m's StepParams for this launch (its tables, buffers, counters and
+// births, and the shared-memory layout of its staged tables).  The plan kernel cuts each model's
+// work items (survivors, then newborns) into runs of 'chunk' items and numbers them: model m owns
+// items [item_begin[m], item_begin[m + 1]).  Each block of the batch kernel takes the next item
+// from item_next, stages its model's tables when they are not the ones it holds, and runs it.
+struct BatchLaunch {
+    const StepParams* params;
+    std::uint32_t* item_begin;   // [n_models + 1], written by the plan kernel
+    std::uint32_t* item_next;    // items handed out, cleared by the plan kernel
+    std::uint32_t n_models;
+    std::uint32_t chunk;
+};
+
 }// namespace psim::gpu

@@ -633,61 +633,46 @@ std::uint64_t Engine::init_builders(double t_eq, double eff_energy, const double
     return total;
 }
 
-void Engine::run(int precision, void* stream_ptr) {
+// Room for at least 'need' phonons of rec_bytes each; the first 'live' records of state buffer
+// 'cur' are kept.  grow_ahead allocates a quarter more than asked (and at least half again the
+// current capacity), for runs that grow their buffers between chunks of launches.
+void Engine::ensure_capacity(std::uint64_t need, std::uint64_t live, int cur, std::size_t rec_bytes, bool grow_ahead, void* stream_ptr) {
     Impl& I = *impl_;
-    const SimDesc& d = desc_;
-    if (!I.builders_ready) { throw std::logic_error("init_builders must be called before run"); }
-    cudaStream_t stream = stream_ptr != nullptr ? static_cast<cudaStream_t>(stream_ptr) : I.own;
-    const bool fp64 = precision != 0;
-    const std::size_t rec_bytes = fp64 ? 64 : 32;
-    // State buffers.  The population never exceeds the phonons created in the run, so a run whose
-    // phonons all fit in kWholeRunStateBytes gets room for every one of them and runs as one CUDA
-    // graph.  A larger run is chunked instead: before each chunk of launches the host reads the
-    // population entering it and grows the buffers when that population plus the chunk's newborns
-    // would not fit, so the buffers follow the peak population and no phonon is ever dropped.
-    const std::uint64_t whole = std::max<std::uint64_t>(I.total + 1024, 4096);
-    const bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
-    if (I.state[0].bytes != I.capacity * rec_bytes) {// first run, or the other precision's records
-        I.state[0].release();
-        I.state[1].release();
-        I.capacity = 0;
+    auto stream = static_cast<cudaStream_t>(stream_ptr);
+    if (need <= I.capacity) { return; }
+    if (need > 0xFFFFFFFFULL) { throw std::length_error("more than 2^32 - 1 phonons in flight"); }
+    std::size_t free_b = 0;
+    std::size_t total_b = 0;
+    check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    const std::uint64_t held = I.capacity * 2 * rec_bytes;
+    const std::uint64_t limit = static_cast<std::uint64_t>((free_b + held) * 0.8) / (2 * rec_bytes);
+    std::uint64_t cap = grow_ahead ? std::max(need + need / 4, I.capacity + I.capacity / 2) : need;
+    cap = std::min<std::uint64_t>(std::min(cap, limit), 0xFFFFFFFFULL);
+    if (cap < need) {
+        throw std::length_error("phonon buffers: " + std::to_string(need) + " phonons in flight do not fit in device memory");
     }
-    // Room for at least 'need' phonons; 'live' records of the buffer 'cur' are kept.
-    auto ensure_capacity = [&](std::uint64_t need, std::uint64_t live, int cur) {
-        if (need <= I.capacity) { return; }
-        if (need > 0xFFFFFFFFULL) { throw std::length_error("more than 2^32 - 1 phonons in flight"); }
-        std::size_t free_b = 0;
-        std::size_t total_b = 0;
-        check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
-        const std::uint64_t held = I.capacity * 2 * rec_bytes;
-        const std::uint64_t limit = static_cast<std::uint64_t>((free_b + held) * 0.8) / (2 * rec_bytes);
-        std::uint64_t cap = chunked ? std::max(need + need / 4, I.capacity + I.capacity / 2) : need;
-        cap = std::min<std::uint64_t>(std::min(cap, limit), 0xFFFFFFFFULL);
-        if (cap < need) {
-            throw std::length_error("phonon buffers: " + std::to_string(need) + " phonons in flight do not fit in device memory");
+    Buf a;
+    Buf b;
+    a.alloc(cap * rec_bytes);
+    b.alloc(cap * rec_bytes);
+    if (live > 0) {// records are SoA: one 16-byte word per phonon per segment of 'capacity' words
+        for (std::size_t k = 0; k < rec_bytes / 16; ++k) {
+            check(cudaMemcpyAsync(static_cast<char*>(a.p) + k * cap * 16, static_cast<const char*>(I.state[cur].p) + k * I.capacity * 16,
+                                  live * 16, cudaMemcpyDeviceToDevice, stream),
+                  "state copy");
         }
-        Buf a;
-        Buf b;
-        a.alloc(cap * rec_bytes);
-        b.alloc(cap * rec_bytes);
-        if (live > 0) {// records are SoA: one 16-byte word per phonon per segment of 'capacity' words
-            for (std::size_t k = 0; k < rec_bytes / 16; ++k) {
-                check(cudaMemcpyAsync(static_cast<char*>(a.p) + k * cap * 16, static_cast<const char*>(I.state[cur].p) + k * I.capacity * 16,
-                                      live * 16, cudaMemcpyDeviceToDevice, stream),
-                      "state copy");
-            }
-            check(cudaStreamSynchronize(stream), "state copy");
-        }
-        I.state[cur].take(a);
-        I.state[1 - cur].take(b);
-        I.capacity = cap;
-    };
-    if (!chunked) { ensure_capacity(whole, 0, 0); }
-    check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
-    check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
-    check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
+        check(cudaStreamSynchronize(stream), "state copy");
+    }
+    I.state[cur].take(a);
+    I.state[1 - cur].take(b);
+    I.capacity = cap;
+}
 
-    StepParams P{};
+// The launch parameters that do not change between a run's launches.
+void Engine::base_params(StepParams& P) const {
+    const Impl& I = *impl_;
+    const SimDesc& d = desc_;
+    P = StepParams{};
     P.cells32 = I.cells32.as<CellF32>();
     P.cells64 = I.cells64.as<CellF64>();
     P.subs64 = I.subs64.as<Sub64>();
@@ -714,6 +699,103 @@ void Engine::run(int precision, void* stream_ptr) {
     P.tally = I.tally.as<TallySlot>();
     P.counters = I.counters.as<unsigned long long>();
     P.population = I.population.as<std::uint32_t>();
+    P.n_cells = d.n_cells;
+    P.n_tables = d.n_tables;
+    P.n_materials = d.n_materials;
+    P.n_emitters = d.n_emitters;
+}
+
+// Launch w of the run: steps [s0, s0 + tw), its state buffers and counters (cycling with w) and
+// the births of each of its steps.
+void Engine::window_params(StepParams& P, std::uint64_t w, std::uint64_t s0, std::uint32_t tw) const {
+    const Impl& I = *impl_;
+    auto* counts = I.counts.as<std::uint32_t>();
+    P.capacity = static_cast<std::uint32_t>(I.capacity);
+    P.step = static_cast<std::uint32_t>(s0);
+    P.n_fused = tw;
+    P.in = I.state[w % 2].p;
+    P.out = I.state[(w + 1) % 2].p;
+    P.count_in = counts + (w % 3);
+    P.count_out = counts + ((w + 1) % 3);
+    P.count_clear = counts + ((w + 2) % 3);
+    P.work = counts + 4 + (w % 3);
+    P.work_clear = counts + 4 + ((w + 2) % 3);
+    P.group_begin = I.group_begin[s0];
+    P.group_end = I.group_begin[s0 + 1];
+    P.n_new = I.n_new[s0];
+    P.id_base = I.id_base[s0];
+    P.new_begin[0] = 0U;
+    for (std::uint32_t j = 0; j < tw; ++j) {
+        P.new_begin[j + 1] = P.new_begin[j] + I.n_new[s0 + j];
+        P.id_base_f[j] = I.id_base[s0 + j];
+        P.group_begin_f[j] = I.group_begin[s0 + j];
+    }
+    P.group_begin_f[tw] = I.group_begin[s0 + tw];
+}
+
+// Steps of launches covering [s0, s0 + cap) whose work items all number in 32 bits.
+std::uint32_t Engine::window_steps(std::uint64_t s0, std::uint32_t cap, std::uint64_t capacity) const {
+    const Impl& I = *impl_;
+    std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(cap, desc_.steps - s0));
+    auto items = [&](std::uint32_t n) {
+        std::uint64_t t = capacity;
+        for (std::uint32_t j = 0; j < n; ++j) { t += I.n_new[s0 + j]; }
+        return t;
+    };
+    while (tw > 1 && items(tw) > 0xFFFFFFFFULL) { --tw; }
+    if (items(tw) > 0xFFFFFFFFULL) { throw std::length_error("too many phonons in one step for 32-bit work indices"); }
+    return tw;
+}
+
+// Reads the run's device counters into the run counters.
+void Engine::finish_run(double ms, std::uint64_t launches, std::uint64_t transport_launches, std::uint32_t fused) {
+    Impl& I = *impl_;
+    unsigned long long c[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    check(cudaMemcpy(c, I.counters.p, sizeof c, cudaMemcpyDeviceToHost), "counters");
+    counters_.phonon_steps += c[0];
+    counters_.relocations += c[1];
+    counters_.event_limits += c[4];
+    counters_.backscatters += c[6];
+    counters_.state_bytes = I.state[0].bytes + I.state[1].bytes;
+    I.builders_ready = false;
+    if (c[5] != 0) { throw std::runtime_error("CUDA staging of the model tables into shared memory timed out"); }
+    counters_.overflow += c[2];
+    counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
+    counters_.kernel_ms += ms;
+    counters_.d2h_bytes += sizeof c;
+    counters_.kernel_launches += launches;
+    counters_.transport_launches += transport_launches;
+    counters_.steps_per_launch = fused;
+    last_fused_ = fused;
+    if (c[2] != 0) { throw std::length_error("phonon buffer overflow: the device ran out of memory for the population"); }
+}
+
+void Engine::run(int precision, void* stream_ptr) {
+    Impl& I = *impl_;
+    const SimDesc& d = desc_;
+    if (!I.builders_ready) { throw std::logic_error("init_builders must be called before run"); }
+    cudaStream_t stream = stream_ptr != nullptr ? static_cast<cudaStream_t>(stream_ptr) : I.own;
+    const bool fp64 = precision != 0;
+    const std::size_t rec_bytes = fp64 ? 64 : 32;
+    // State buffers.  The population never exceeds the phonons created in the run, so a run whose
+    // phonons all fit in kWholeRunStateBytes gets room for every one of them and runs as one CUDA
+    // graph.  A larger run is chunked instead: before each chunk of launches the host reads the
+    // population entering it and grows the buffers when that population plus the chunk's newborns
+    // would not fit, so the buffers follow the peak population and no phonon is ever dropped.
+    const std::uint64_t whole = std::max<std::uint64_t>(I.total + 1024, 4096);
+    const bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
+    if (I.state[0].bytes != I.capacity * rec_bytes) {// first run, or the other precision's records
+        I.state[0].release();
+        I.state[1].release();
+        I.capacity = 0;
+    }
+    if (!chunked) { ensure_capacity(whole, 0, 0, rec_bytes, false, stream); }
+    check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
+    check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
+    check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
+
+    StepParams P{};
+    base_params(P);
     auto* counts = I.counts.as<std::uint32_t>();
     // Launch shape and shared memory.  The FP32 kernel stages the cell records and the
     // alias / velocity / bin-centre tables into shared memory (TMA bulk copies) when they fit
@@ -727,10 +809,6 @@ void Engine::run(int precision, void* stream_ptr) {
     P.coast_lanes = coast_lanes_;
     if (const char* c = std::getenv("PSIM_GB300_COAST"); c != nullptr) { P.coast_lanes = static_cast<std::uint32_t>(std::max(0, std::atoi(c))); }
     std::size_t tally_b = tally_smem_bytes(d.n_sensors, 1);
-    P.n_cells = d.n_cells;
-    P.n_tables = d.n_tables;
-    P.n_materials = d.n_materials;
-    P.n_emitters = d.n_emitters;
     P.stage_mask = 0U;
     P.off_tally = 0U;
     std::size_t smem = tally_b;
@@ -803,37 +881,9 @@ void Engine::run(int precision, void* stream_ptr) {
     std::uint64_t launches = 0;
     std::uint64_t w = 0;
     auto enqueue = [&](std::uint64_t from, std::uint64_t to) {
-        P.capacity = static_cast<std::uint32_t>(I.capacity);
         for (std::uint64_t s0 = from; s0 < to; ++w) {
-            std::uint32_t tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, to - s0));
-            // every work item of a launch is numbered in 32 bits
-            auto items = [&](std::uint32_t n) {
-                std::uint64_t t = P.capacity;
-                for (std::uint32_t j = 0; j < n; ++j) { t += I.n_new[s0 + j]; }
-                return t;
-            };
-            while (tw > 1 && items(tw) > 0xFFFFFFFFULL) { --tw; }
-            if (items(tw) > 0xFFFFFFFFULL) { throw std::length_error("too many phonons in one step for 32-bit work indices"); }
-            P.step = static_cast<std::uint32_t>(s0);
-            P.n_fused = tw;
-            P.in = I.state[w % 2].p;
-            P.out = I.state[(w + 1) % 2].p;
-            P.count_in = counts + (w % 3);
-            P.count_out = counts + ((w + 1) % 3);
-            P.count_clear = counts + ((w + 2) % 3);
-            P.work = counts + 4 + (w % 3);
-            P.work_clear = counts + 4 + ((w + 2) % 3);
-            P.group_begin = I.group_begin[s0];
-            P.group_end = I.group_begin[s0 + 1];
-            P.n_new = I.n_new[s0];
-            P.id_base = I.id_base[s0];
-            P.new_begin[0] = 0U;
-            for (std::uint32_t j = 0; j < tw; ++j) {
-                P.new_begin[j + 1] = P.new_begin[j] + I.n_new[s0 + j];
-                P.id_base_f[j] = I.id_base[s0 + j];
-                P.group_begin_f[j] = I.group_begin[s0 + j];
-            }
-            P.group_begin_f[tw] = I.group_begin[s0 + tw];
+            std::uint32_t tw = window_steps(s0, static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, to - s0)), I.capacity);
+            window_params(P, w, s0, tw);
             if (fp64) {
                 launch_step_f64(P, grid, smem, stream);
             } else {
@@ -873,7 +923,8 @@ void Engine::run(int precision, void* stream_ptr) {
                 check(cudaMemcpyAsync(&live, counts + (w % 3), sizeof live, cudaMemcpyDeviceToHost, stream), "count read");
                 check(cudaStreamSynchronize(stream), "count read");
             }
-            ensure_capacity(static_cast<std::uint64_t>(live) + (born[to] - born[done]) + 1024, live, static_cast<int>(w % 2));
+            ensure_capacity(static_cast<std::uint64_t>(live) + (born[to] - born[done]) + 1024, live, static_cast<int>(w % 2), rec_bytes, true,
+                            stream);
             enqueue(done, to);
             check(cudaGetLastError(), "step launch");
             done = to;
@@ -910,24 +961,7 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     float ms = 0.f;
     check(cudaEventElapsedTime(&ms, I.ev0, I.ev1), "event time");
-    unsigned long long c[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
-    check(cudaMemcpy(c, I.counters.p, sizeof c, cudaMemcpyDeviceToHost), "counters");
-    counters_.phonon_steps += c[0];
-    counters_.relocations += c[1];
-    counters_.event_limits += c[4];
-    counters_.backscatters += c[6];
-    counters_.state_bytes = I.state[0].bytes + I.state[1].bytes;
-    if (c[5] != 0) { throw std::runtime_error("CUDA staging of the model tables into shared memory timed out"); }
-    counters_.overflow += c[2];
-    counters_.max_population = std::max<std::uint64_t>(counters_.max_population, c[3]);
-    counters_.kernel_ms += ms;
-    counters_.d2h_bytes += sizeof c;
-    counters_.kernel_launches += launches + checks;
-    counters_.transport_launches += fp64 ? launches : launches - 1;// FP32 adds one population pass
-    counters_.steps_per_launch = fused;
-    last_fused_ = fused;
-    I.builders_ready = false;
-    if (c[2] != 0) { throw std::length_error("phonon buffer overflow: the device ran out of memory for the population"); }
+    finish_run(ms, launches + checks, fp64 ? launches : launches - 1, fused);// FP32 adds one population pass
 }
 
 void Engine::set_steady_stop(bool on, const SteadyCriterion& c, std::uint64_t check_every) {

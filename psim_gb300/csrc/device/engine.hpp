@@ -10,6 +10,8 @@
 
 namespace psim::gpu {
 
+struct StepParams;
+
 constexpr std::uint32_t kMaxMaterialsHost = 16;
 
 // Owning copy of psim_sim_desc (include/psim_gb300.h).
@@ -130,7 +132,23 @@ public:
     const SimDesc& desc() const noexcept { return desc_; }
     void* stream() const noexcept { return stream_; }
 
+    // Runs the transport of every engine's prepared run (init_builders done) in one sequence of
+    // batched launches on `stream`: each launch covers the same window of steps for every model,
+    // and its blocks take runs of one model's phonons from a device work queue (FP32 kernel,
+    // `per_thread` phonons per thread in a work item).  Returns false, having run nothing, when the
+    // engines cannot share launches (different step counts, a steady-state stop, or a model whose
+    // tables and tallies do not fit the batched kernel's shared memory).  Each engine's run then
+    // finishes as after run(): its counters hold its own phonon-steps, and kernel_ms the batch's
+    // device time split by phonon-steps.
+    static bool run_batched(const std::vector<Engine*>& engines, void* stream, std::uint32_t per_thread = 16);
+
 private:
+    void ensure_capacity(std::uint64_t need, std::uint64_t live, int cur, std::size_t rec_bytes, bool grow_ahead, void* stream);
+    void base_params(StepParams& P) const;
+    void window_params(StepParams& P, std::uint64_t w, std::uint64_t s0, std::uint32_t tw) const;
+    std::uint32_t window_steps(std::uint64_t s0, std::uint32_t cap, std::uint64_t capacity) const;
+    void finish_run(double ms, std::uint64_t launches, std::uint64_t transport_launches, std::uint32_t fused);
+
     struct Impl;
     SimDesc desc_;
     std::unique_ptr<Impl> impl_;

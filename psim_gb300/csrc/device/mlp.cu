@@ -1,7 +1,8 @@
 // The warm-start surrogate's multilayer perceptron: BF16 parameters and activations, FP32
 // accumulation, GELU hidden layers, a linear output, mean-squared-error loss and Adam with FP32
 // master weights.  Everything runs in a handful of hand-written kernels:
-//   gemm_kernel      C = op(A) op(B) from BF16 tiles staged in shared memory, FP32 sums
+//   gemm_kernel      C = op(A) op(B) on the tensor cores (mma.sync m16n8k16, BF16 operands staged
+//                    in shared memory, FP32 sums)
 //   bias_act_kernel  Z = C + b, and the BF16 activation GELU(Z) (hidden) or Z (output)
 //   mse_kernel       dY = 2 (Y - T) / (n outputs), and the loss
 //   gelu_bwd_kernel  dZ = dA GELU'(Z)
@@ -10,6 +11,8 @@
 // The network is small (about 0.5 M parameters): a step is a few microseconds of GPU time.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 #include <algorithm>
 #include <cmath>
@@ -58,34 +61,104 @@ template<typename T> struct DevArray {
     }
 };
 
-constexpr int kTile = 16;
+// GEMM tiles: a 64 x 64 block of C per 128-thread block (four warps of 32 x 32), K in steps of
+// 16.  Operand tiles are staged in shared memory as BF16 with k contiguous, zero-padded at the
+// matrix edges, and multiplied on the tensor cores by mma.sync m16n8k16 (BF16 in, FP32 sums).
+constexpr int kBM = 64;
+constexpr int kBN = 64;
+constexpr int kBK = 16;
+constexpr int kPadK = kBK + 8;// row pitch in elements: 48 bytes, so the fragment loads of a warp spread over the banks
+
+// One m16n8k16 product: c += a (16 x 16, row-major fragment) b (16 x 8, column-major fragment).
+__device__ __forceinline__ void mma_bf16_16816(float c[4], const std::uint32_t a[4], const std::uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, {%0, %1, %2, %3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
 
 // C[M][N] = op(A)[M][K] op(B)[K][N].  op(A)(m, k) = A[k*M + m] when transA else A[m*K + k];
 // op(B)(k, n) = B[n*K + k] when transB else B[k*N + n].
-__global__ void gemm_kernel(const __nv_bfloat16* A, const __nv_bfloat16* B, float* C, int M, int N, int K, bool transA,
-                            bool transB) {
-    __shared__ float As[kTile][kTile + 1];
-    __shared__ float Bs[kTile][kTile + 1];
-    const int tx = static_cast<int>(threadIdx.x);
-    const int ty = static_cast<int>(threadIdx.y);
-    const int m = static_cast<int>(blockIdx.y) * kTile + ty;
-    const int n = static_cast<int>(blockIdx.x) * kTile + tx;
-    float acc = 0.f;
-    for (int k0 = 0; k0 < K; k0 += kTile) {
-        const int ka = k0 + tx;// A tile: row m, column ka
-        const int kb = k0 + ty;// B tile: row kb, column n
-        float a = 0.f;
-        float b = 0.f;
-        if (m < M && ka < K) { a = __bfloat162float(transA ? A[static_cast<std::size_t>(ka) * M + m] : A[static_cast<std::size_t>(m) * K + ka]); }
-        if (kb < K && n < N) { b = __bfloat162float(transB ? B[static_cast<std::size_t>(n) * K + kb] : B[static_cast<std::size_t>(kb) * N + n]); }
-        As[ty][tx] = a;
-        Bs[ty][tx] = b;
-        __syncthreads();
+__global__ void __launch_bounds__(128) gemm_kernel(const __nv_bfloat16* A, const __nv_bfloat16* B, float* C, int M, int N, int K,
+                                                   bool transA, bool transB) {
+    __shared__ __align__(16) __nv_bfloat16 As[kBM][kPadK];// [m][k]
+    __shared__ __align__(16) __nv_bfloat16 Bs[kBN][kPadK];// [n][k]
+    const int tid = static_cast<int>(threadIdx.x);
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+    const int group = lane >> 2;// fragment row (A, C) or column (B)
+    const int tig = lane & 3;   // thread in group: fragment k pair (A, B) or column pair (C)
+    const int m0 = static_cast<int>(blockIdx.y) * kBM;
+    const int n0 = static_cast<int>(blockIdx.x) * kBN;
+    const int wm = (warp >> 1) * 32;// the warp's 32 x 32 sub-tile
+    const int wn = (warp & 1) * 32;
+    const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+    float acc[2][4][4];
 #pragma unroll
-        for (int k = 0; k < kTile; ++k) { acc = fmaf(As[ty][k], Bs[k][tx], acc); }
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) { acc[i][j][r] = 0.f; }
+        }
+    }
+    for (int k0 = 0; k0 < K; k0 += kBK) {
+        // stage op(A)[m0.., k0..] and op(B)[k0.., n0..] (transposed to [n][k]): 8 elements each per thread
+#pragma unroll
+        for (int e = 0; e < (kBM * kBK) / 128; ++e) {
+            const int idx = tid + e * 128;
+            const int r = idx / kBK;
+            const int k = idx % kBK;
+            const int m = m0 + r;
+            const int kk = k0 + k;
+            __nv_bfloat16 v = zero;
+            if (m < M && kk < K) { v = transA ? A[static_cast<std::size_t>(kk) * M + m] : A[static_cast<std::size_t>(m) * K + kk]; }
+            As[r][k] = v;
+            const int n = n0 + r;
+            __nv_bfloat16 w = zero;
+            if (n < N && kk < K) { w = transB ? B[static_cast<std::size_t>(n) * K + kk] : B[static_cast<std::size_t>(kk) * N + n]; }
+            Bs[r][k] = w;
+        }
+        __syncthreads();
+        std::uint32_t af[2][4];
+        std::uint32_t bf[4][2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {// A fragments: rows group / group + 8, k pairs 2 tig / 2 tig + 8
+            const int r = wm + i * 16 + group;
+            af[i][0] = *reinterpret_cast<const std::uint32_t*>(&As[r][2 * tig]);
+            af[i][1] = *reinterpret_cast<const std::uint32_t*>(&As[r + 8][2 * tig]);
+            af[i][2] = *reinterpret_cast<const std::uint32_t*>(&As[r][2 * tig + 8]);
+            af[i][3] = *reinterpret_cast<const std::uint32_t*>(&As[r + 8][2 * tig + 8]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {// B fragments: column group, k pairs 2 tig / 2 tig + 8
+            const int c = wn + j * 8 + group;
+            bf[j][0] = *reinterpret_cast<const std::uint32_t*>(&Bs[c][2 * tig]);
+            bf[j][1] = *reinterpret_cast<const std::uint32_t*>(&Bs[c][2 * tig + 8]);
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { mma_bf16_16816(acc[i][j], af[i], bf[j]); }
+        }
         __syncthreads();
     }
-    if (m < M && n < N) { C[static_cast<std::size_t>(m) * N + n] = acc; }
+    // C fragments: rows group / group + 8, columns 2 tig, 2 tig + 1
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int r = m0 + wm + i * 16 + group;
+            const int c = n0 + wn + j * 8 + 2 * tig;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int rr = r + h * 8;
+                if (rr >= M) { continue; }
+                if (c < N) { C[static_cast<std::size_t>(rr) * N + c] = acc[i][j][2 * h]; }
+                if (c + 1 < N) { C[static_cast<std::size_t>(rr) * N + c + 1] = acc[i][j][2 * h + 1]; }
+            }
+        }
+    }
 }
 
 __device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
@@ -248,9 +321,8 @@ void Mlp::set_params(const float* in) {
 namespace {
 
 void gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, float* C, int M, int N, int K, bool tA, bool tB, cudaStream_t s) {
-    const dim3 block(kTile, kTile);
-    const dim3 grid(static_cast<unsigned>((N + kTile - 1) / kTile), static_cast<unsigned>((M + kTile - 1) / kTile));
-    gemm_kernel<<<grid, block, 0, s>>>(A, B, C, M, N, K, tA, tB);
+    const dim3 grid(static_cast<unsigned>((N + kBN - 1) / kBN), static_cast<unsigned>((M + kBM - 1) / kBM));
+    gemm_kernel<<<grid, 128, 0, s>>>(A, B, C, M, N, K, tA, tB);
 }
 
 // Buffers for batches of up to B rows.

@@ -16,6 +16,8 @@
 // reference: Cell::handleSurfaceCollision -> CompositeSurface::handlePhonon
 // (psim/src/cell.cpp:103-108, psim/src/compositeSurface.cpp:47-66) resolves each edge
 // to its first transition surface, else its first emitting surface, else the boundary.
+#include <algorithm>
+
 #include "transport.cuh"
 
 namespace psim::gpu {
@@ -481,57 +483,15 @@ template<unsigned S> __device__ __forceinline__ bool segment32(const StepParams&
     return false;
 }
 
-// Persistent lanes: each lane pulls the next phonon of the step (alive phonons first, then the
-// steps' newborns) from a warp-aggregated work counter and advances it one segment per
-// iteration.  A phonon that crosses a boundary into another of the launch's steps stays in its
-// lane; one that leaves the launch (or dies) frees the lane for the next work item.  The warp
-// stays full until the launch's work runs out instead of waiting for its slowest phonon.
-// P is a __grid_constant__ so the per-step arrays in it are read in place with a runtime index.
-template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const __grid_constant__ StepParams P) {
-    __shared__ std::uint64_t stage_bar;
-    if constexpr (S != 0U) {// TMA bulk copies of the read-only tables into shared memory
-        if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            const unsigned cells_b = (S & kStageCells) ? P.n_cells * static_cast<unsigned>(sizeof(CellF32)) : 0U;
-            const unsigned alias_b = P.n_tables * kAliasCols * 4U;
-            const unsigned vel_b = P.n_materials * 2U * kBins * 4U;
-            const unsigned centre_b = P.n_materials * kBins * 4U;
-            const unsigned sens_b = P.n_sensors * static_cast<unsigned>(sizeof(SensorDev));
-            const unsigned mat_b = P.n_materials * static_cast<unsigned>(sizeof(MaterialDev));
-            const unsigned emit_b = P.n_emitters * static_cast<unsigned>(sizeof(EmitterDev));
-            mbar_expect_tx(&stage_bar, cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b);
-            bulk_to_shared(g_smem + P.off_sensors, P.sensors, sens_b, &stage_bar);
-            bulk_to_shared(g_smem + P.off_materials, P.materials, mat_b, &stage_bar);
-            if (emit_b != 0U) { bulk_to_shared(g_smem + P.off_emitters, P.emitters, emit_b, &stage_bar); }
-            if (cells_b != 0U) { bulk_to_shared(g_smem + P.off_cells, P.cells32, cells_b, &stage_bar); }
-            bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, &stage_bar);
-            bulk_to_shared(g_smem + P.off_vel, P.vel32, vel_b, &stage_bar);
-            bulk_to_shared(g_smem + P.off_centre, P.centre32, centre_b, &stage_bar);
-        }
-    }
-    BlockTally bt;
-    tally_init(P, bt, g_smem, P.n_fused);
-    if constexpr (S != 0U) {
-        const bool ok = mbar_wait_bounded(&stage_bar);
-        if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
-            if (threadIdx.x == 0) { atomicAdd(P.counters + 5, 1ULL); }
-            mbar_wait_bounded(&stage_bar);
-            return;
-        }
-    }
-    const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
-    if (blockIdx.x == 0) {
-        if (threadIdx.x == 0) {
-            *P.count_clear = 0U;
-            *P.work_clear = 0U;
-        }
-        // each step's population: its newborns here, the phonons crossing into it in window_add
-        if (threadIdx.x < P.n_fused) {
-            atomicAdd(P.population + P.step + threadIdx.x, P.new_begin[threadIdx.x + 1U] - P.new_begin[threadIdx.x]);
-        }
-    }
-    const std::uint32_t total = n_alive + P.new_begin[P.n_fused];
+// Persistent lanes over the work items [first, total) of one model's launch (survivors entering
+// the launch's first step below n_alive, then the steps' newborns): each lane takes the next item
+// from 'fetch' (a warp-aggregated counter: fetch(k) hands out k consecutive items and returns the
+// first) and advances it one segment per iteration.  A phonon that crosses a boundary into another
+// of the launch's steps stays in its lane; one that leaves the launch (or dies) frees the lane for
+// the next item, so the warp stays full until the items run out instead of waiting for its
+// slowest phonon.  Returns the phonon-steps of this thread.
+template<unsigned S, bool kCoast, typename Fetch>
+__device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uint32_t n_alive, std::uint32_t total, Fetch fetch) {
     const unsigned full = 0xFFFFFFFFU;
     std::uint32_t steps = 0;// phonon-steps of this thread (a launch gives each thread far fewer than 2^32)
     bool active = false;
@@ -544,7 +504,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(
             if (need != 0U) {
                 const int leader = __ffs(static_cast<int>(need)) - 1;
                 std::uint32_t base = 0;
-                if (static_cast<int>(threadIdx.x & 31U) == leader) { base = atomicAdd(P.work, static_cast<std::uint32_t>(__popc(need))); }
+                if (static_cast<int>(threadIdx.x & 31U) == leader) { base = fetch(static_cast<std::uint32_t>(__popc(need))); }
                 base = __shfl_sync(full, base, leader);
                 if (base + static_cast<std::uint32_t>(__popc(need)) >= total) { exhausted = true; }
                 if (!active) {
@@ -562,7 +522,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(
         // Plain boundaries first, in a loop the warp runs while enough of its lanes cross one: a
         // phonon on its way into the launch's next step stays here, so the segment below is
         // mostly the phonon's next event (an impact, a scattering event, a new scattering time).
-        if (P.coast_lanes != 0U) {
+        if (kCoast) {
             bool coasting = active;
             while (true) {
                 Outcome c{ false, false, false, false, 0U, 0, 0 };
@@ -588,7 +548,8 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(
             }
         }
         if (active && !done) {
-            if (L.rs.left == 0) { L.rs.prefill(); }// most segments here draw: make the words together
+            // after a coasting loop most segments here draw: make their words together
+            if (kCoast && L.rs.left == 0) { L.rs.prefill(); }
             done = segment32<S>(P, L, o);
         }
         const bool finishing = active && done;
@@ -608,8 +569,167 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(
             active = false;
         }
     }
+    return steps;
+}
+
+// Issues the TMA bulk copies of one model's read-only tables into the block's shared memory
+// (the layout in P's offsets), completing on 'bar' (one thread).
+template<unsigned S> __device__ __forceinline__ void stage_tables(const StepParams& P, std::uint64_t* bar) {
+    const unsigned cells_b = (S & kStageCells) ? P.n_cells * static_cast<unsigned>(sizeof(CellF32)) : 0U;
+    const unsigned alias_b = P.n_tables * kAliasCols * 4U;
+    const unsigned vel_b = P.n_materials * 2U * kBins * 4U;
+    const unsigned centre_b = P.n_materials * kBins * 4U;
+    const unsigned sens_b = P.n_sensors * static_cast<unsigned>(sizeof(SensorDev));
+    const unsigned mat_b = P.n_materials * static_cast<unsigned>(sizeof(MaterialDev));
+    const unsigned emit_b = P.n_emitters * static_cast<unsigned>(sizeof(EmitterDev));
+    mbar_expect_tx(bar, cells_b + alias_b + vel_b + centre_b + sens_b + mat_b + emit_b);
+    bulk_to_shared(g_smem + P.off_sensors, P.sensors, sens_b, bar);
+    bulk_to_shared(g_smem + P.off_materials, P.materials, mat_b, bar);
+    if (emit_b != 0U) { bulk_to_shared(g_smem + P.off_emitters, P.emitters, emit_b, bar); }
+    if (cells_b != 0U) { bulk_to_shared(g_smem + P.off_cells, P.cells32, cells_b, bar); }
+    bulk_to_shared(g_smem + P.off_alias, P.alias, alias_b, bar);
+    bulk_to_shared(g_smem + P.off_vel, P.vel32, vel_b, bar);
+    bulk_to_shared(g_smem + P.off_centre, P.centre32, centre_b, bar);
+}
+
+// One model's launch: the blocks stage the model's tables, then their lanes share the launch's
+// work items through one global counter (lanes_run).  P is a __grid_constant__ so the per-step
+// arrays in it are read in place with a runtime index.
+template<unsigned S, bool kCoast> __global__ void __launch_bounds__(1024, 1) step_kernel_f32(const __grid_constant__ StepParams P) {
+    __shared__ std::uint64_t stage_bar;
+    if constexpr (S != 0U) {// TMA bulk copies of the read-only tables into shared memory
+        if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
+        __syncthreads();
+        if (threadIdx.x == 0) { stage_tables<S>(P, &stage_bar); }
+    }
+    BlockTally bt;
+    tally_init(P, bt, g_smem, P.n_fused);
+    if constexpr (S != 0U) {
+        const bool ok = mbar_wait_bounded(&stage_bar);
+        if (__syncthreads_or(!ok)) {// the copy did not complete: leave this step's work to other blocks
+            if (threadIdx.x == 0) { atomicAdd(P.counters + 5, 1ULL); }
+            mbar_wait_bounded(&stage_bar);
+            return;
+        }
+    }
+    const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) {
+            *P.count_clear = 0U;
+            *P.work_clear = 0U;
+        }
+        // each step's population: its newborns here, the phonons crossing into it in window_add
+        if (threadIdx.x < P.n_fused) {
+            atomicAdd(P.population + P.step + threadIdx.x, P.new_begin[threadIdx.x + 1U] - P.new_begin[threadIdx.x]);
+        }
+    }
+    const std::uint32_t total = n_alive + P.new_begin[P.n_fused];
+    const std::uint32_t steps = lanes_run<S, kCoast>(P, n_alive, total, [&](std::uint32_t k) { return atomicAdd(P.work, k); });
     block_count_add(P.counters + 0, static_cast<unsigned long long>(steps));
     window_flush(P, g_smem);
+}
+
+// Numbers the work items of a batched launch (one block): model m's survivors entering the
+// window plus the window's newborns, in runs of B.chunk items, at [item_begin[m], item_begin[m+1]).
+// It also does for every model what block 0 of a single model's launch does: clear the counters of
+// two launches ahead and add each step's newborns to its population.
+__global__ void batch_plan_kernel(const __grid_constant__ BatchLaunch B) {
+    for (std::uint32_t m = threadIdx.x; m < B.n_models; m += blockDim.x) {
+        const StepParams& P = B.params[m];
+        *P.count_clear = 0U;
+        *P.work_clear = 0U;
+        for (std::uint32_t j = 0; j < P.n_fused; ++j) { atomicAdd(P.population + P.step + j, P.new_begin[j + 1U] - P.new_begin[j]); }
+    }
+    if (threadIdx.x == 0) {
+        std::uint32_t acc = 0;
+        for (std::uint32_t m = 0; m < B.n_models; ++m) {
+            const StepParams& P = B.params[m];
+            B.item_begin[m] = acc;
+            const std::uint32_t n = min(*P.count_in, P.capacity) + P.new_begin[P.n_fused];
+            acc += (n + B.chunk - 1U) / B.chunk;
+        }
+        B.item_begin[B.n_models] = acc;
+        *B.item_next = 0U;
+    }
+}
+
+// The batched launch: persistent blocks take work items (a run of one model's phonons) in order.
+// A block stages an item's model (its StepParams into shared memory, its tables by TMA, a cleared
+// tally) when it is not the model the block holds, after flushing the previous model's tally and
+// phonon-step count; its lanes then share the item's phonons through a shared-memory counter
+// (lanes_run).  Results equal the model's own launches: a phonon's random stream is keyed by
+// (seed, step, id), and tallies are exact integer sums.
+template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32(const __grid_constant__ BatchLaunch B) {
+    __shared__ std::uint64_t stage_bar;
+    __shared__ __align__(16) StepParams sP;
+    __shared__ std::uint32_t s_model, s_lo, s_hi, s_alive, s_next;
+    if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
+    __syncthreads();
+    const std::uint32_t n_items = B.item_begin[B.n_models];
+    constexpr std::uint32_t kNone = 0xFFFFFFFFU;
+    std::uint32_t staged = kNone;
+    unsigned parity = 0U;
+    std::uint32_t steps = 0;
+    while (true) {
+        if (threadIdx.x == 0) {
+            const std::uint32_t it = atomicAdd(B.item_next, 1U);
+            std::uint32_t m = kNone;
+            std::uint32_t lo = 0;
+            std::uint32_t hi = 0;
+            std::uint32_t alive = 0;
+            if (it < n_items) {// the model owning item 'it': the last m with item_begin[m] <= it
+                std::uint32_t a = 0;
+                std::uint32_t b = B.n_models;
+                while (b - a > 1U) {
+                    const std::uint32_t mid = (a + b) >> 1;
+                    if (B.item_begin[mid] <= it) {
+                        a = mid;
+                    } else {
+                        b = mid;
+                    }
+                }
+                m = a;
+                const StepParams& P = B.params[m];
+                alive = min(*P.count_in, P.capacity);
+                const std::uint32_t total = alive + P.new_begin[P.n_fused];
+                lo = (it - B.item_begin[m]) * B.chunk;
+                hi = min(lo + B.chunk, total);
+            }
+            s_model = m;
+            s_lo = lo;
+            s_hi = hi;
+            s_alive = alive;
+            s_next = 0U;
+        }
+        __syncthreads();
+        const std::uint32_t m = s_model;
+        if (m != staged) {
+            if (staged != kNone) {// the previous model's tally and phonon-steps
+                block_count_add(sP.counters + 0, static_cast<unsigned long long>(steps));
+                steps = 0;
+                window_flush(sP, g_smem);
+                __syncthreads();
+            }
+            if (m == kNone) { break; }
+            const auto* src = reinterpret_cast<const std::uint32_t*>(B.params + m);
+            auto* dst = reinterpret_cast<std::uint32_t*>(&sP);
+            for (std::uint32_t i = threadIdx.x; i < sizeof(StepParams) / 4U; i += blockDim.x) { dst[i] = src[i]; }
+            __syncthreads();
+            if (threadIdx.x == 0) { stage_tables<S>(sP, &stage_bar); }
+            BlockTally bt;
+            tally_init(sP, bt, g_smem, sP.n_fused);
+            const bool ok = mbar_wait_bounded(&stage_bar, parity);
+            parity ^= 1U;
+            if (__syncthreads_or(!ok)) {// the copy did not complete: stop this block (reported)
+                if (threadIdx.x == 0) { atomicAdd(sP.counters + 5, 1ULL); }
+                mbar_wait_bounded(&stage_bar, parity ^ 1U);
+                return;
+            }
+            staged = m;
+        }
+        steps += lanes_run<S, false>(sP, s_alive, s_hi, [&](std::uint32_t k) { return s_lo + atomicAdd(&s_next, k); });
+        __syncthreads();
+    }
 }
 
 // The FP32 rates on given inputs (a known-answer check against Material::relaxRates).
@@ -641,29 +761,42 @@ void launch_population_max(const std::uint32_t* population, std::uint32_t n, uns
     population_max_kernel<<<1, 1024, 0, stream>>>(population, n, counters);
 }
 
-// The kernel variant of a staging mask (0, tables only, or everything).
-const void* step_f32_fn(unsigned stage_mask) {
-    if (stage_mask == (kStageCells | kStageTables)) { return reinterpret_cast<const void*>(step_kernel_f32<kStageCells | kStageTables>); }
-    if (stage_mask == kStageTables) { return reinterpret_cast<const void*>(step_kernel_f32<kStageTables>); }
-    return reinterpret_cast<const void*>(step_kernel_f32<0U>);
+// The kernel variant of a staging mask (0, tables only, or everything) and coasting choice.
+template<bool C> const void* step_f32_fn_c(unsigned stage_mask) {
+    if (stage_mask == (kStageCells | kStageTables)) { return reinterpret_cast<const void*>(step_kernel_f32<kStageCells | kStageTables, C>); }
+    if (stage_mask == kStageTables) { return reinterpret_cast<const void*>(step_kernel_f32<kStageTables, C>); }
+    return reinterpret_cast<const void*>(step_kernel_f32<0U, C>);
+}
+const void* step_f32_fn(unsigned stage_mask, bool coast) { return coast ? step_f32_fn_c<true>(stage_mask) : step_f32_fn_c<false>(stage_mask); }
+
+template<bool C> void launch_f32_c(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
+    if (P.stage_mask == (kStageCells | kStageTables)) {
+        step_kernel_f32<kStageCells | kStageTables, C><<<grid, block, smem, stream>>>(P);
+    } else if (P.stage_mask == kStageTables) {
+        step_kernel_f32<kStageTables, C><<<grid, block, smem, stream>>>(P);
+    } else {
+        step_kernel_f32<0U, C><<<grid, block, smem, stream>>>(P);
+    }
 }
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream) {
-    if (P.stage_mask == (kStageCells | kStageTables)) {
-        step_kernel_f32<kStageCells | kStageTables><<<grid, block, smem, stream>>>(P);
-    } else if (P.stage_mask == kStageTables) {
-        step_kernel_f32<kStageTables><<<grid, block, smem, stream>>>(P);
+    if (P.coast_lanes != 0U) {
+        launch_f32_c<true>(P, grid, block, smem, stream);
     } else {
-        step_kernel_f32<0U><<<grid, block, smem, stream>>>(P);
+        launch_f32_c<false>(P, grid, block, smem, stream);
     }
+}
+
+void launch_batch_f32(const BatchLaunch& B, int grid, std::size_t smem, cudaStream_t stream) {
+    batch_plan_kernel<<<1, 1024, 0, stream>>>(B);
+    batch_kernel_f32<kStageCells | kStageTables><<<grid, 1024, smem, stream>>>(B);
 }
 
 // Blocks per multiprocessor for this launch shape, 0 when it cannot launch.  The kernel's
 // dynamic shared-memory limit is a process-wide attribute: it is always raised to the device's
 // maximum (the same value for every caller), never to one model's need, so engines that run
 // side by side on other threads cannot lower it under each other's launches.
-int occupancy_f32(unsigned stage_mask, int block, std::size_t smem) {
-    const void* fn = step_f32_fn(stage_mask);
+int occupancy_of(const void* fn, int block, std::size_t smem) {
     int dev = 0;
     int optin = 0;
     cudaFuncAttributes fa{};
@@ -684,6 +817,24 @@ int occupancy_f32(unsigned stage_mask, int block, std::size_t smem) {
         return 0;
     }
     return blocks;
+}
+
+int occupancy_batch_f32(std::size_t smem) {
+    return occupancy_of(reinterpret_cast<const void*>(batch_kernel_f32<kStageCells | kStageTables>), 1024, smem);
+}
+
+// Static shared memory of the batched kernel (its StepParams copy among it).
+std::size_t batch_static_smem() {
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(batch_kernel_f32<kStageCells | kStageTables>)) != cudaSuccess) {
+        cudaGetLastError();
+        return sizeof(StepParams) + 1024;
+    }
+    return fa.sharedSizeBytes;
+}
+
+int occupancy_f32(unsigned stage_mask, int block, std::size_t smem) {
+    return std::min(occupancy_of(step_f32_fn(stage_mask, false), block, smem), occupancy_of(step_f32_fn(stage_mask, true), block, smem));
 }
 
 }// namespace psim::gpu

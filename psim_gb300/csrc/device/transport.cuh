@@ -98,10 +98,11 @@ __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parit
     return ok != 0U;
 }
 
-// Bounded wait for phase 0 of the staging barrier; false after the iteration limit.
-__device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar) {
+// Bounded wait for the phase of the staging barrier with the given parity (0 for its first use);
+// false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar, unsigned parity = 0U) {
     for (unsigned it = 0; it < (1U << 22); ++it) {
-        if (mbar_try_wait(bar, 0U)) { return true; }
+        if (mbar_try_wait(bar, parity)) { return true; }
     }
     return false;
 }
