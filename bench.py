@@ -461,7 +461,8 @@ def main():
             models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in zip(ids, paths)]
             if opt is None:
                 opt, tuned_rate = api.batch_autotune(models, sample=min(8, len(models)))
-            s_c, n_c = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
+            s_c, n_c = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks,
+                                     device_queue=bool(opt.device_queue), per_thread=opt.per_thread)
             secs += s_c
             steps_b += n_c
             if single is None:

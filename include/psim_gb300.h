@@ -148,23 +148,31 @@ void psim_mlp_destroy(psim_mlp* net);
 
 /* ------------------------------------------------------------------------------------------
  * Many independent models on one GPU.  No counterpart in the reference, which runs one model
- * per process (psim/src/main.cpp:10-31 loops over its input files).  A host work queue hands
- * the models to `workers` threads, each with its own CUDA stream; each model runs as
- * psim_model_run would (its own seed, precision and steady-state stop), its transport launches
- * limited to `max_blocks` thread blocks so that small models share the GPU.  A model's results
- * do not depend on the batch it ran in.
+ * per process (psim/src/main.cpp:10-31 loops over its input files).  Each model runs as
+ * psim_model_run would (its own seed, precision and steady-state stop).  With device_queue set,
+ * the FP32 models of the batch that have the same number of steps share their transport: one
+ * CUDA graph of batched launches, each covering one window of steps for every model, whose
+ * persistent thread blocks take runs of `per_thread` x 1024 phonons of one model at a time from
+ * a device work queue and stage that model's tables in shared memory.  Worker threads prepare
+ * and interpret the runs.  The other models (FP64, a steady-state stop, tables beyond the
+ * kernel's shared memory, or device_queue 0) run on `workers` host threads, each with its own
+ * CUDA stream, their transport launches limited to `max_blocks` thread blocks.  A model's
+ * results do not depend on the batch it ran in.
  * ------------------------------------------------------------------------------------------ */
 typedef struct psim_batch_options {
-    int32_t workers;    /* host threads, one CUDA stream each (>= 1) */
-    int32_t max_blocks; /* thread blocks per transport launch (0: one per multiprocessor) */
+    int32_t workers;      /* host threads (>= 1) */
+    int32_t max_blocks;   /* thread blocks per transport launch of a model run on its own (0: one per multiprocessor) */
+    int32_t device_queue; /* 1: batched launches fed by a device work queue where the models allow */
+    int32_t per_thread;   /* batched launches: phonons per thread in one work item (>= 1) */
 } psim_batch_options;
 /* Runs every model once; fails with the first model's failure after the others stopped.
  * seconds (may be NULL): wall time; phonon_steps (may be NULL): over all models. */
 int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_options* opt, double* seconds,
                    uint64_t* phonon_steps);
-/* The autotuner: runs the first `sample` models under each candidate (workers 4, 8, 16, 32 x blocks
- * per launch 1/8, 1/4, 1/2 and all of the multiprocessors) and returns the fastest options and
- * their rate (phonon-steps/s; may be NULL). */
+/* The autotuner: runs the first `sample` models under each candidate (batched launches with 4, 8,
+ * 16 or 32 phonons per thread in a work item; models on their own under workers 4, 8, 16, 32 x
+ * blocks per launch 1/8, 1/4, 1/2 and all of the multiprocessors) and returns the fastest options
+ * and their rate (phonon-steps/s; may be NULL). */
 int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, psim_batch_options* out,
                         double* best_rate);
 
@@ -339,7 +347,9 @@ int psim_sim_steps_run(const psim_sim* s, uint64_t* steps);
  * work overlaps (different streams, or several host threads) race on it and give wrong results;
  * order them on one stream or with events.  The first call on each device looks up the
  * scratch's address (and may load the module onto that device): make it before any stream
- * capture. */
+ * capture.  Whether the call can be captured in a CUDA graph is not covered here.  The address is
+ * kept per device ordinal for the life of the process, so hosts that reset a device
+ * (cudaDeviceReset) or run in a context other than the device's primary one are not supported. */
 int psim_final_temps_noalloc(const psim_interp_desc* d, const int64_t* energy_dev, uint64_t start_step,
                              double* out_dev, void* cuda_stream);
 /* Size in bytes of the fixed scratch behind psim_final_temps_noalloc. */

@@ -83,7 +83,8 @@ class InterpDesc(ctypes.Structure):
 
 
 class BatchOptions(ctypes.Structure):
-    _fields_ = [("workers", ctypes.c_int32), ("max_blocks", ctypes.c_int32)]
+    _fields_ = [("workers", ctypes.c_int32), ("max_blocks", ctypes.c_int32), ("device_queue", ctypes.c_int32),
+                ("per_thread", ctypes.c_int32)]
 
 
 # Every symbol the C header declares, with (restype, argtypes).
@@ -478,9 +479,11 @@ def _handles(models):
     return arr
 
 
-def batch_run(models, workers: int = 8, max_blocks: int = 0) -> Tuple[float, int]:
-    """Runs every Model once, concurrently (psim_batch_run): (wall seconds, phonon-steps)."""
-    opt = BatchOptions(workers, max_blocks)
+def batch_run(models, workers: int = 8, max_blocks: int = 0, device_queue: bool = True,
+              per_thread: int = 16) -> Tuple[float, int]:
+    """Runs every Model once, together (psim_batch_run): (wall seconds, phonon-steps).  With
+    device_queue the FP32 models share batched launches fed by a device work queue."""
+    opt = BatchOptions(workers, max_blocks, 1 if device_queue else 0, per_thread)
     secs = ctypes.c_double()
     steps = ctypes.c_uint64()
     _check(lib().psim_batch_run(_handles(models), len(models), ctypes.byref(opt), ctypes.byref(secs),

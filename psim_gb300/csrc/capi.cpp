@@ -562,6 +562,8 @@ int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_option
         psim::BatchOptions o;
         o.workers = opt->workers;
         o.max_blocks = opt->max_blocks;
+        o.device_queue = opt->device_queue;
+        o.per_thread = opt->per_thread;
         const psim::BatchResult r = psim::run_batch(batch_models(models, n), o);
         if (seconds != nullptr) { *seconds = r.seconds; }
         if (phonon_steps != nullptr) { *phonon_steps = r.phonon_steps; }
@@ -574,6 +576,8 @@ int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, ps
         const psim::BatchOptions o = psim::autotune_batch(batch_models(models, n), sample, best_rate);
         out->workers = o.workers;
         out->max_blocks = o.max_blocks;
+        out->device_queue = o.device_queue;
+        out->per_thread = o.per_thread;
     });
 }
 

@@ -278,6 +278,16 @@ struct StepParams {
     const std::uint32_t* count_in;
     std::uint32_t* count_out;
     std::uint32_t* count_clear;
+    // FP32 survivors may be written in two groups: the front group from slot 0 up (count_*), the
+    // back group from slot capacity - 1 down (back_*), by the key sort_mode picks (0: front only;
+    // 1: back when the time to the next scattering event is below sort_after ns; 2: back when
+    // the group velocity is at least sort_after m/s), so that the next launch hands its lanes
+    // runs of phonons alike.  Work item i < *count_in is slot i, the others are the back group.
+    const std::uint32_t* back_in;
+    std::uint32_t* back_out;
+    std::uint32_t* back_clear;
+    std::uint32_t sort_mode;
+    float sort_after;
     std::uint32_t* work;              // this step's work counter (phonons handed to lanes)
     std::uint32_t* work_clear;        // the counter of two steps ahead, cleared by this step
     std::uint32_t* population;        // [n_steps] phonons in flight per step (FP32: accumulated, zeroed per run)

@@ -21,6 +21,9 @@
 namespace psim::gpu {
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
+void launch_batch_f32(const BatchLaunch& B, int grid, std::size_t smem, cudaStream_t stream);
+int occupancy_batch_f32(std::size_t smem);
+std::size_t batch_static_smem();
 void launch_population_max(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters, cudaStream_t stream);
 void launch_step_f64(const StepParams& P, int grid, std::size_t smem, cudaStream_t stream);
 void launch_rates32(const MaterialDev& m, const SensorDev* s, const float* w, const int* pol, int n, double* out, cudaStream_t stream);
@@ -314,7 +317,7 @@ struct Engine::Impl {
     Buf d_groups;
     Buf state[2];
     std::uint64_t capacity{ 0 };
-    Buf counts;  // 3 x u32
+    Buf counts;  // u32: survivor counters [0, 3), work counters [4, 7), back-group survivor counters [8, 11)
     Buf counters;// 8 x u64: phonon-steps, relocations, overflow, max population, event-limit hits
     Buf tally;   // [K][S]
     Buf population;// [N] u32
@@ -528,7 +531,7 @@ Engine::Engine(const SimDesc& d)
     model_bytes_ = I.cells32.bytes + I.cells64.bytes + I.subs64.bytes + I.materials.bytes + I.centre32.bytes + I.vel32.bytes
                    + I.centre64.bytes + I.vel64.bytes + I.alias.bytes + I.sensors.bytes + I.emitters.bytes;
     // ---- run buffers
-    I.counts.alloc(8 * sizeof(std::uint32_t));// 3 survivor counters, 3 work counters
+    I.counts.alloc(16 * sizeof(std::uint32_t));// 3 survivor counters, 3 work counters, 3 back-group counters
     I.counters.alloc(8 * sizeof(unsigned long long));
     I.tally.alloc(static_cast<std::size_t>(d.recorded) * d.n_sensors * sizeof(TallySlot));
     I.population.alloc(static_cast<std::size_t>(d.steps) * sizeof(std::uint32_t));
@@ -633,10 +636,12 @@ std::uint64_t Engine::init_builders(double t_eq, double eff_energy, const double
     return total;
 }
 
-// Room for at least 'need' phonons of rec_bytes each; the first 'live' records of state buffer
-// 'cur' are kept.  grow_ahead allocates a quarter more than asked (and at least half again the
-// current capacity), for runs that grow their buffers between chunks of launches.
-void Engine::ensure_capacity(std::uint64_t need, std::uint64_t live, int cur, std::size_t rec_bytes, bool grow_ahead, void* stream_ptr) {
+// Room for at least 'need' phonons of rec_bytes each; the records of state buffer 'cur' are kept:
+// its first live_front slots and its last live_back slots (the two groups of survivors).
+// grow_ahead allocates a quarter more than asked (and at least half again the current capacity),
+// for runs that grow their buffers between chunks of launches.
+void Engine::ensure_capacity(std::uint64_t need, std::uint64_t live_front, std::uint64_t live_back, int cur, std::size_t rec_bytes,
+                             bool grow_ahead, void* stream_ptr) {
     Impl& I = *impl_;
     auto stream = static_cast<cudaStream_t>(stream_ptr);
     if (need <= I.capacity) { return; }
@@ -655,11 +660,16 @@ void Engine::ensure_capacity(std::uint64_t need, std::uint64_t live, int cur, st
     Buf b;
     a.alloc(cap * rec_bytes);
     b.alloc(cap * rec_bytes);
-    if (live > 0) {// records are SoA: one 16-byte word per phonon per segment of 'capacity' words
+    if (live_front + live_back > 0) {// records are SoA: one 16-byte word per phonon per segment of 'capacity' words
         for (std::size_t k = 0; k < rec_bytes / 16; ++k) {
-            check(cudaMemcpyAsync(static_cast<char*>(a.p) + k * cap * 16, static_cast<const char*>(I.state[cur].p) + k * I.capacity * 16,
-                                  live * 16, cudaMemcpyDeviceToDevice, stream),
-                  "state copy");
+            const char* src = static_cast<const char*>(I.state[cur].p) + k * I.capacity * 16;
+            char* dst = static_cast<char*>(a.p) + k * cap * 16;
+            if (live_front > 0) { check(cudaMemcpyAsync(dst, src, live_front * 16, cudaMemcpyDeviceToDevice, stream), "state copy"); }
+            if (live_back > 0) {
+                check(cudaMemcpyAsync(dst + (cap - live_back) * 16, src + (I.capacity - live_back) * 16, live_back * 16,
+                                      cudaMemcpyDeviceToDevice, stream),
+                      "state copy");
+            }
         }
         check(cudaStreamSynchronize(stream), "state copy");
     }
@@ -720,6 +730,9 @@ void Engine::window_params(StepParams& P, std::uint64_t w, std::uint64_t s0, std
     P.count_clear = counts + ((w + 2) % 3);
     P.work = counts + 4 + (w % 3);
     P.work_clear = counts + 4 + ((w + 2) % 3);
+    P.back_in = counts + 8 + (w % 3);
+    P.back_out = counts + 8 + ((w + 1) % 3);
+    P.back_clear = counts + 8 + ((w + 2) % 3);
     P.group_begin = I.group_begin[s0];
     P.group_end = I.group_begin[s0 + 1];
     P.n_new = I.n_new[s0];
@@ -783,13 +796,14 @@ void Engine::run(int precision, void* stream_ptr) {
     // population entering it and grows the buffers when that population plus the chunk's newborns
     // would not fit, so the buffers follow the peak population and no phonon is ever dropped.
     const std::uint64_t whole = std::max<std::uint64_t>(I.total + 1024, 4096);
-    const bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
+    bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
+    if (const char* ch = std::getenv("PSIM_GB300_CHUNKED"); ch != nullptr && std::atoi(ch) != 0) { chunked = true; }// test switch
     if (I.state[0].bytes != I.capacity * rec_bytes) {// first run, or the other precision's records
         I.state[0].release();
         I.state[1].release();
         I.capacity = 0;
     }
-    if (!chunked) { ensure_capacity(whole, 0, 0, rec_bytes, false, stream); }
+    if (!chunked) { ensure_capacity(whole, 0, 0, 0, rec_bytes, false, stream); }
     check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
     check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
     check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
@@ -807,6 +821,19 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     std::uint32_t fused = 1;
     P.coast_lanes = coast_lanes_;
+    P.sort_mode = 0U;
+    if (const char* so = std::getenv("PSIM_GB300_SORT"); so != nullptr && !fp64) {// "mode:value", value in steps or m/s
+        const int mode = std::atoi(so);
+        const char* colon = std::strchr(so, ':');
+        const double v = colon != nullptr ? std::atof(colon + 1) : 0.;
+        if (mode == 1) {
+            P.sort_mode = 1U;
+            P.sort_after = static_cast<float>(v * P.dt64);
+        } else if (mode == 2) {
+            P.sort_mode = 2U;
+            P.sort_after = static_cast<float>(v);
+        }
+    }
     if (const char* c = std::getenv("PSIM_GB300_COAST"); c != nullptr) { P.coast_lanes = static_cast<std::uint32_t>(std::max(0, std::atoi(c))); }
     std::size_t tally_b = tally_smem_bytes(d.n_sensors, 1);
     P.stage_mask = 0U;
@@ -918,13 +945,14 @@ void Engine::run(int precision, void* stream_ptr) {
             std::uint64_t to = std::min<std::uint64_t>(d.steps, done + kLaunchesPerChunk * fused);
             if (stop_on_) { to = std::min(to, next_check); }
             // the phonons entering step 'done' (the next launch's input count) plus the chunk's newborns
-            std::uint32_t live = 0;
+            std::uint32_t live[2] = { 0U, 0U };// the front and back groups of survivors
             if (done > 0) {
-                check(cudaMemcpyAsync(&live, counts + (w % 3), sizeof live, cudaMemcpyDeviceToHost, stream), "count read");
+                check(cudaMemcpyAsync(&live[0], counts + (w % 3), sizeof(std::uint32_t), cudaMemcpyDeviceToHost, stream), "count read");
+                check(cudaMemcpyAsync(&live[1], counts + 8 + (w % 3), sizeof(std::uint32_t), cudaMemcpyDeviceToHost, stream), "count read");
                 check(cudaStreamSynchronize(stream), "count read");
             }
-            ensure_capacity(static_cast<std::uint64_t>(live) + (born[to] - born[done]) + 1024, live, static_cast<int>(w % 2), rec_bytes, true,
-                            stream);
+            ensure_capacity(static_cast<std::uint64_t>(live[0]) + live[1] + (born[to] - born[done]) + 1024, live[0], live[1],
+                            static_cast<int>(w % 2), rec_bytes, true, stream);
             enqueue(done, to);
             check(cudaGetLastError(), "step launch");
             done = to;
@@ -962,6 +990,155 @@ void Engine::run(int precision, void* stream_ptr) {
     float ms = 0.f;
     check(cudaEventElapsedTime(&ms, I.ev0, I.ev1), "event time");
     finish_run(ms, launches + checks, fp64 ? launches : launches - 1, fused);// FP32 adds one population pass
+}
+
+bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, std::uint32_t per_thread) {
+    if (engines.empty()) { return true; }
+    auto stream = static_cast<cudaStream_t>(stream_ptr);
+    const std::uint64_t steps = engines.front()->desc_.steps;
+    int dev = 0;
+    int optin = 0;
+    check(cudaGetDevice(&dev), "cudaGetDevice");
+    check(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "device attribute");
+    const std::size_t budget = static_cast<std::size_t>(optin) - batch_static_smem() - 256;
+    std::uint32_t fuse_cap = kMaxFused;
+    if (const char* f = std::getenv("PSIM_GB300_FUSE"); f != nullptr && std::atoi(f) > 0) {
+        fuse_cap = std::min<std::uint32_t>(kMaxFused, static_cast<std::uint32_t>(std::atoi(f)));
+    }
+    // every model's tables and a shared tally of `fused` slots in one block's shared memory
+    struct Layout {
+        std::size_t cells, alias, vel, centre, sens, mat, emit;
+        std::size_t tables() const { return cells + alias + vel + centre + sens + mat + emit; }
+    };
+    std::vector<Layout> lay(engines.size());
+    std::uint32_t fused = fuse_cap;
+    for (std::size_t e = 0; e < engines.size(); ++e) {
+        const Engine& E = *engines[e];
+        const SimDesc& d = E.desc_;
+        if (!E.impl_->builders_ready || d.steps != steps || E.stop_on_ || d.n_sensors > static_cast<std::uint32_t>(kSharedSensors)) {
+            return false;
+        }
+        Layout& L = lay[e];
+        L.cells = static_cast<std::size_t>(d.n_cells) * sizeof(CellF32);
+        L.alias = static_cast<std::size_t>(d.n_tables) * kAliasCols * 4;
+        L.vel = static_cast<std::size_t>(d.n_materials) * 2 * kBins * 4;
+        L.centre = static_cast<std::size_t>(d.n_materials) * kBins * 4;
+        L.sens = static_cast<std::size_t>(d.n_sensors) * sizeof(SensorDev);
+        L.mat = static_cast<std::size_t>(d.n_materials) * sizeof(MaterialDev);
+        L.emit = static_cast<std::size_t>(d.n_emitters) * sizeof(EmitterDev);
+        while (fused > 1 && L.tables() + tally_smem_bytes(d.n_sensors, fused) > budget) { --fused; }
+        if (L.tables() + tally_smem_bytes(d.n_sensors, fused) > budget) { return false; }
+    }
+    std::size_t smem = 0;
+    for (std::size_t e = 0; e < engines.size(); ++e) {
+        smem = std::max(smem, lay[e].tables() + tally_smem_bytes(engines[e]->desc_.n_sensors, fused));
+    }
+    const int occ = occupancy_batch_f32(smem);
+    if (occ <= 0) { return false; }
+    const int grid = engines.front()->impl_->sms * occ;
+
+    // state buffers for every phonon of each run, cleared counters
+    for (Engine* E : engines) {
+        Impl& I = *E->impl_;
+        if (I.state[0].bytes != I.capacity * 32) {
+            I.state[0].release();
+            I.state[1].release();
+            I.capacity = 0;
+        }
+        E->ensure_capacity(std::max<std::uint64_t>(I.total + 1024, 4096), 0, 0, 0, 32, false, stream);
+        check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
+        check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
+        check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
+    }
+    // each launch's parameters of every model: params[w][m]
+    const std::size_t M = engines.size();
+    std::vector<std::uint64_t> starts;
+    for (std::uint64_t s0 = 0; s0 < steps; s0 += fused) { starts.push_back(s0); }
+    std::vector<StepParams> params(starts.size() * M);
+    for (std::size_t m = 0; m < M; ++m) {
+        const Engine& E = *engines[m];
+        const Layout& L = lay[m];
+        StepParams base{};
+        E.base_params(base);
+        base.coast_lanes = 0U;
+        base.stage_mask = 7U;
+        base.off_cells = 0U;
+        base.off_alias = static_cast<std::uint32_t>(L.cells);
+        base.off_vel = static_cast<std::uint32_t>(L.cells + L.alias);
+        base.off_centre = static_cast<std::uint32_t>(L.cells + L.alias + L.vel);
+        base.off_sensors = static_cast<std::uint32_t>(L.cells + L.alias + L.vel + L.centre);
+        base.off_materials = static_cast<std::uint32_t>(base.off_sensors + L.sens);
+        base.off_emitters = static_cast<std::uint32_t>(base.off_materials + L.mat);
+        base.off_tally = static_cast<std::uint32_t>(L.tables());
+        for (std::size_t w = 0; w < starts.size(); ++w) {
+            StepParams P = base;
+            const std::uint64_t s0 = starts[w];
+            const auto tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, steps - s0));
+            if (E.window_steps(s0, tw, E.impl_->capacity) != tw) { return false; }// numbering beyond 32 bits
+            E.window_params(P, w, s0, tw);
+            params[w * M + m] = P;
+        }
+    }
+    Buf d_params;
+    Buf d_items;
+    d_params.upload(params);
+    d_items.alloc((M + 2) * sizeof(std::uint32_t));
+    BatchLaunch B{};
+    B.item_begin = d_items.as<std::uint32_t>();
+    B.item_next = d_items.as<std::uint32_t>() + M + 1;
+    B.n_models = static_cast<std::uint32_t>(M);
+    B.chunk = std::max<std::uint32_t>(1U, per_thread) * 1024U;
+
+    cudaEvent_t ev0 = nullptr;
+    cudaEvent_t ev1 = nullptr;
+    check(cudaEventCreate(&ev0), "event");
+    check(cudaEventCreate(&ev1), "event");
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    float ms = 0.f;
+    try {
+        check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        for (std::size_t w = 0; w < starts.size(); ++w) {
+            B.params = d_params.as<StepParams>() + w * M;
+            launch_batch_f32(B, grid, smem, stream);
+        }
+        for (Engine* E : engines) {
+            Impl& I = *E->impl_;
+            launch_population_max(I.population.as<std::uint32_t>(), static_cast<std::uint32_t>(steps), I.counters.as<unsigned long long>(),
+                                  stream);
+        }
+        check(cudaStreamEndCapture(stream, &graph), "end capture");
+        check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+        check(cudaEventRecord(ev0, stream), "event record");
+        check(cudaGraphLaunch(exec, stream), "graph launch");
+        check(cudaEventRecord(ev1, stream), "event record");
+        check(cudaStreamSynchronize(stream), "batch sync");
+        check(cudaEventElapsedTime(&ms, ev0, ev1), "event time");
+    } catch (...) {
+        if (exec != nullptr) { cudaGraphExecDestroy(exec); }
+        if (graph != nullptr) { cudaGraphDestroy(graph); }
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        throw;
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    // each run's counters; the batch's device time split by phonon-steps
+    std::vector<unsigned long long> st(M, 0ULL);
+    unsigned long long all = 0;
+    for (std::size_t m = 0; m < M; ++m) {
+        check(cudaMemcpy(&st[m], engines[m]->impl_->counters.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost), "counters");
+        all += st[m];
+    }
+    for (std::size_t m = 0; m < M; ++m) {
+        const double share = all > 0 ? static_cast<double>(st[m]) / static_cast<double>(all) : 1. / static_cast<double>(M);
+        engines[m]->steps_run_ = steps;
+        engines[m]->last_stage_mask_ = 7U;
+        engines[m]->finish_run(ms * share, 2 * starts.size() + 1, starts.size(), fused);
+    }
+    return true;
 }
 
 void Engine::set_steady_stop(bool on, const SteadyCriterion& c, std::uint64_t check_every) {

@@ -143,7 +143,8 @@ public:
     static bool run_batched(const std::vector<Engine*>& engines, void* stream, std::uint32_t per_thread = 16);
 
 private:
-    void ensure_capacity(std::uint64_t need, std::uint64_t live, int cur, std::size_t rec_bytes, bool grow_ahead, void* stream);
+    void ensure_capacity(std::uint64_t need, std::uint64_t live_front, std::uint64_t live_back, int cur, std::size_t rec_bytes,
+                         bool grow_ahead, void* stream);
     void base_params(StepParams& P) const;
     void window_params(StepParams& P, std::uint64_t w, std::uint64_t s0, std::uint32_t tw) const;
     std::uint32_t window_steps(std::uint64_t s0, std::uint32_t cap, std::uint64_t capacity) const;

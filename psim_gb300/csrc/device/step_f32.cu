@@ -249,8 +249,9 @@ __device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, st
 template<unsigned S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive) {
     if (i < n_alive) {
         const float4* in_pd = static_cast<const float4*>(P.in);
-        const float4 a = in_pd[i];
-        const uint4 b = reinterpret_cast<const uint4*>(in_pd + P.capacity)[i];
+        const std::uint32_t slot = slot_of(P, i);
+        const float4 a = in_pd[slot];
+        const uint4 b = reinterpret_cast<const uint4*>(in_pd + P.capacity)[slot];
         L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
         lane_enter_step(P, L, P.step);
     } else {
@@ -556,7 +557,8 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
         const bool crossing = finishing && o.alive;// into step L.step + 1
         const bool stays = crossing && o.cont;
         steps += (finishing && o.boundary) ? 1U : 0U;
-        const std::uint32_t slot = reserve_slot(P, crossing && !stays);
+        const bool back = P.sort_mode == 1U ? L.p.tts < P.sort_after : (P.sort_mode == 2U && L.v >= P.sort_after);
+        const std::uint32_t slot = reserve_slot(P, crossing && !stays, back);
         if (slot != 0xFFFFFFFFU) {// records: float4 {px, py, dx, dy}[capacity], then uint4 {meta, binw, tts, id}[capacity]
             float4* out_pd = static_cast<float4*>(P.out);
             out_pd[slot] = make_float4(L.p.px, L.p.py, L.p.dx, L.p.dy);
@@ -612,11 +614,14 @@ template<unsigned S, bool kCoast> __global__ void __launch_bounds__(1024, 1) ste
             return;
         }
     }
-    const std::uint32_t n_alive = min(*P.count_in, P.capacity);// survivors beyond the buffer were dropped and counted
+    const std::uint32_t n_alive = alive_in(P);
     if (blockIdx.x == 0) {
         if (threadIdx.x == 0) {
             *P.count_clear = 0U;
+            *P.back_clear = 0U;
             *P.work_clear = 0U;
+            const std::uint32_t both = *P.count_in + *P.back_in;
+            if (both > P.capacity) { atomicAdd(P.counters + 2, static_cast<unsigned long long>(both - P.capacity)); }
         }
         // each step's population: its newborns here, the phonons crossing into it in window_add
         if (threadIdx.x < P.n_fused) {
@@ -637,7 +642,10 @@ __global__ void batch_plan_kernel(const __grid_constant__ BatchLaunch B) {
     for (std::uint32_t m = threadIdx.x; m < B.n_models; m += blockDim.x) {
         const StepParams& P = B.params[m];
         *P.count_clear = 0U;
+        *P.back_clear = 0U;
         *P.work_clear = 0U;
+        const std::uint32_t both = *P.count_in + *P.back_in;
+        if (both > P.capacity) { atomicAdd(P.counters + 2, static_cast<unsigned long long>(both - P.capacity)); }
         for (std::uint32_t j = 0; j < P.n_fused; ++j) { atomicAdd(P.population + P.step + j, P.new_begin[j + 1U] - P.new_begin[j]); }
     }
     if (threadIdx.x == 0) {
@@ -645,7 +653,7 @@ __global__ void batch_plan_kernel(const __grid_constant__ BatchLaunch B) {
         for (std::uint32_t m = 0; m < B.n_models; ++m) {
             const StepParams& P = B.params[m];
             B.item_begin[m] = acc;
-            const std::uint32_t n = min(*P.count_in, P.capacity) + P.new_begin[P.n_fused];
+            const std::uint32_t n = alive_in(P) + P.new_begin[P.n_fused];
             acc += (n + B.chunk - 1U) / B.chunk;
         }
         B.item_begin[B.n_models] = acc;
@@ -690,7 +698,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
                 }
                 m = a;
                 const StepParams& P = B.params[m];
-                alive = min(*P.count_in, P.capacity);
+                alive = alive_in(P);
                 const std::uint32_t total = alive + P.new_begin[P.n_fused];
                 lo = (it - B.item_begin[m]) * B.chunk;
                 hi = min(lo + B.chunk, total);

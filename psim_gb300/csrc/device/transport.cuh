@@ -209,21 +209,39 @@ inline std::size_t tally_smem_bytes(std::uint32_t S, std::uint32_t slots = 1) {
     return ((static_cast<std::size_t>(S) * slots * 20 + kMaxFused * 4 + 15) / 16) * 16;
 }
 
-// Warp-aggregated slot reservation in the output buffer; returns the slot or UINT32_MAX.
-__device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool alive) {
+// Warp-aggregated slot reservation in the output buffer, in the front group (from slot 0 up) or,
+// with 'back', the back group (from the last slot down); returns the slot or UINT32_MAX.
+__device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool alive, bool back = false) {
     const unsigned full = 0xFFFFFFFFU;
-    const unsigned mask = __ballot_sync(full, alive);
+    const unsigned front_mask = __ballot_sync(full, alive && !back);
+    const unsigned back_mask = __ballot_sync(full, alive && back);
     const int lane = static_cast<int>(threadIdx.x & 31U);
     std::uint32_t base = 0;
-    if (lane == 0 && mask != 0U) { base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(mask))); }
+    std::uint32_t base_back = 0;
+    if (lane == 0) {
+        if (front_mask != 0U) { base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(front_mask))); }
+        if (back_mask != 0U) { base_back = atomicAdd(P.back_out, static_cast<std::uint32_t>(__popc(back_mask))); }
+    }
     base = __shfl_sync(full, base, 0);
+    base_back = __shfl_sync(full, base_back, 0);
     if (!alive) { return 0xFFFFFFFFU; }
-    const std::uint32_t slot = base + static_cast<std::uint32_t>(__popc(mask & ((1U << lane) - 1U)));
-    if (slot >= P.capacity) {
+    const unsigned below = (1U << lane) - 1U;
+    const std::uint32_t idx = back ? base_back + static_cast<std::uint32_t>(__popc(back_mask & below))
+                                   : base + static_cast<std::uint32_t>(__popc(front_mask & below));
+    if (idx >= P.capacity) {
         atomicAdd(P.counters + 2, 1ULL);
         return 0xFFFFFFFFU;
     }
-    return slot;
+    return back ? P.capacity - 1U - idx : idx;
+}
+
+// Survivors entering a launch (both groups; beyond the buffer they were dropped and counted).
+__device__ __forceinline__ std::uint32_t alive_in(const StepParams& P) { return min(*P.count_in + *P.back_in, P.capacity); }
+
+// Buffer slot of survivor i: the front group first, then the back group from the last slot down.
+__device__ __forceinline__ std::uint32_t slot_of(const StepParams& P, std::uint32_t i) {
+    const std::uint32_t nf = *P.count_in;
+    return i < nf ? i : P.capacity - 1U - (i - nf);
 }
 
 __device__ __forceinline__ void block_count_add(unsigned long long* target, unsigned long long v) {

@@ -4,6 +4,7 @@
 #include <atomic>
 #include <chrono>
 #include <exception>
+#include <map>
 #include <mutex>
 #include <stdexcept>
 #include <thread>
@@ -13,24 +14,44 @@
 
 namespace psim {
 
-BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions& opt) {
-    if (opt.workers < 1) { throw std::invalid_argument("a batch needs at least one worker"); }
-    if (opt.max_blocks < 0) { throw std::invalid_argument("blocks per launch must not be negative"); }
-    for (const HostModel* m : models) {
-        if (m == nullptr) { throw std::invalid_argument("null model in the batch"); }
-    }
-    for (std::size_t i = 0; i < models.size(); ++i) {
-        for (std::size_t j = i + 1; j < models.size(); ++j) {
-            if (models[i] == models[j]) { throw std::invalid_argument("a model appears twice in the batch"); }
+namespace {
+
+// Runs f(i) for i in [0, n) on up to `workers` threads; rethrows the first failure.
+template<typename F> void parallel_for(std::size_t n, int workers, F f) {
+    std::atomic<std::size_t> next{ 0 };
+    std::mutex err_mu;
+    std::exception_ptr first_error;
+    std::atomic<bool> failed{ false };
+    auto work = [&]() {
+        try {
+            while (!failed.load()) {
+                const std::size_t i = next.fetch_add(1);
+                if (i >= n) { break; }
+                f(i);
+            }
+        } catch (...) {
+            std::lock_guard<std::mutex> lock(err_mu);
+            if (!first_error) { first_error = std::current_exception(); }
+            failed.store(true);
         }
-    }
+    };
+    const int t = std::max(1, std::min<int>(workers, static_cast<int>(n)));
+    std::vector<std::thread> pool;
+    pool.reserve(static_cast<std::size_t>(t));
+    for (int w = 0; w < t; ++w) { pool.emplace_back(work); }
+    for (auto& th : pool) { th.join(); }
+    if (first_error) { std::rethrow_exception(first_error); }
+}
+
+// Every model on its own: worker threads with a CUDA stream each.
+std::uint64_t run_each(const std::vector<HostModel*>& models, const BatchOptions& opt) {
+    if (models.empty()) { return 0; }
     const int workers = std::max(1, std::min<int>(opt.workers, static_cast<int>(models.size())));
     std::atomic<std::size_t> next{ 0 };
     std::atomic<std::uint64_t> steps{ 0 };
     std::mutex err_mu;
     std::exception_ptr first_error;
     std::atomic<bool> failed{ false };
-    const auto t0 = std::chrono::steady_clock::now();
     auto work = [&]() {
         void* stream = nullptr;
         try {
@@ -66,9 +87,69 @@ BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions&
     for (int w = 0; w < workers; ++w) { pool.emplace_back(work); }
     for (auto& t : pool) { t.join(); }
     if (first_error) { std::rethrow_exception(first_error); }
+    return steps.load();
+}
+
+// The models' transports in batched launches, grouped by their number of steps; run by run
+// (models with more runs go on alone after the others finish theirs).
+std::uint64_t run_queued(const std::vector<HostModel*>& models, const BatchOptions& opt) {
+    std::map<std::size_t, std::vector<HostModel*>> groups;
+    for (HostModel* m : models) { groups[m->n_steps()].push_back(m); }
+    std::uint64_t steps = 0;
+    void* stream = gpu::create_stream();
+    try {
+        for (auto& [n_steps, group] : groups) {
+            (void)n_steps;
+            for (HostModel* m : group) { m->begin_runs(); }
+            std::size_t max_runs = 0;
+            for (HostModel* m : group) { max_runs = std::max(max_runs, m->n_runs()); }
+            for (std::size_t r = 0; r < max_runs; ++r) {
+                std::vector<HostModel*> members;
+                for (HostModel* m : group) {
+                    if (m->n_runs() > r) { members.push_back(m); }
+                }
+                parallel_for(members.size(), opt.workers, [&](std::size_t i) { members[i]->prepare_run(r); });
+                std::vector<gpu::Engine*> engines;
+                for (HostModel* m : members) { engines.push_back(m->engine()); }
+                if (!gpu::Engine::run_batched(engines, stream, static_cast<std::uint32_t>(std::max(1, opt.per_thread)))) {
+                    for (HostModel* m : members) { m->engine()->run(m->precision(), stream); }
+                }
+                parallel_for(members.size(), opt.workers, [&](std::size_t i) { members[i]->finish_run(); });
+            }
+            for (HostModel* m : group) {
+                m->end_runs();
+                steps += m->counters().phonon_steps;
+            }
+        }
+    } catch (...) {
+        gpu::destroy_stream(stream);
+        throw;
+    }
+    gpu::destroy_stream(stream);
+    return steps;
+}
+
+}// namespace
+
+BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions& opt) {
+    if (opt.workers < 1) { throw std::invalid_argument("a batch needs at least one worker"); }
+    if (opt.max_blocks < 0) { throw std::invalid_argument("blocks per launch must not be negative"); }
+    if (opt.per_thread < 1) { throw std::invalid_argument("a work item needs at least one phonon per thread"); }
+    for (const HostModel* m : models) {
+        if (m == nullptr) { throw std::invalid_argument("null model in the batch"); }
+    }
+    for (std::size_t i = 0; i < models.size(); ++i) {
+        for (std::size_t j = i + 1; j < models.size(); ++j) {
+            if (models[i] == models[j]) { throw std::invalid_argument("a model appears twice in the batch"); }
+        }
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<HostModel*> queued;
+    std::vector<HostModel*> alone;
+    for (HostModel* m : models) { (opt.device_queue != 0 && m->precision() == 0 && !m->steady_stop() ? queued : alone).push_back(m); }
     BatchResult r;
+    r.phonon_steps = run_queued(queued, opt) + run_each(alone, opt);
     r.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    r.phonon_steps = steps.load();
     return r;
 }
 
@@ -79,10 +160,23 @@ BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, d
     const int sms = gpu::sm_count();
     BatchOptions best;
     double best_r = -1.;
-    for (const int workers : { 4, 8, 16, 32 }) {
+    for (const int per_thread : { 4, 8, 16, 32 }) {// batched launches
+        BatchOptions o;
+        o.workers = 16;
+        o.device_queue = 1;
+        o.per_thread = per_thread;
+        const BatchResult r = run_batch(pilot, o);
+        const double rate = r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;
+        if (rate > best_r) {
+            best_r = rate;
+            best = o;
+        }
+    }
+    for (const int workers : { 4, 8, 16, 32 }) {// every model on its own
         for (const int div : { 8, 4, 2, 1 }) {
             BatchOptions o;
             o.workers = workers;
+            o.device_queue = 0;
             o.max_blocks = std::max(1, sms / div);
             const BatchResult r = run_batch(pilot, o);
             const double rate = r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;

@@ -1,10 +1,14 @@
 // Many independent models on one GPU (the batched workload: uneven cell and phonon counts).
 //
-// psim runs one model per process.  Here a host work queue hands models to worker threads,
-// each with its own non-blocking CUDA stream; every model's run is the usual CUDA graph of
-// transport launches on its worker's stream, with its launches limited to `max_blocks` thread
-// blocks so that small models occupy a few multiprocessors and several run at once.  A model's
-// results do not depend on the stream, the grid or what runs beside it.
+// psim runs one model per process.  Here the FP32 models of a batch that have the same number of
+// steps run their transport together: one CUDA graph of batched launches, each covering the same
+// window of steps for every model, whose persistent blocks take runs of one model's phonons from
+// a device work queue and stage that model's tables in shared memory (gpu::Engine::run_batched).
+// Worker threads prepare the runs (tables, phonon builders) and interpret them afterwards.  Models
+// that cannot share launches (FP64, a steady-state stop, tables beyond the kernel's shared
+// memory) run on the worker threads instead, each with its own CUDA stream and its launches
+// limited to `max_blocks` blocks.  A model's results do not depend on the batch, the stream or
+// the grid: a phonon's random stream is keyed by (seed, step, id) and tallies are exact sums.
 #pragma once
 
 #include <cstdint>
@@ -15,8 +19,10 @@ namespace psim {
 class HostModel;
 
 struct BatchOptions {
-    int workers{ 8 };     // host threads, one CUDA stream each
-    int max_blocks{ 0 };  // thread blocks per transport launch (0: one per multiprocessor)
+    int workers{ 8 };       // host threads, one CUDA stream each
+    int max_blocks{ 0 };    // thread blocks per transport launch of a model run on its own (0: one per multiprocessor)
+    int device_queue{ 1 };  // 1: batched launches fed by a device work queue where models allow; 0: every model on its own
+    int per_thread{ 16 };   // batched launches: phonons per thread in one work item
 };
 
 struct BatchResult {
@@ -28,8 +34,10 @@ struct BatchResult {
 // Throws the first failure after every worker has stopped.
 BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions& opt);
 
-// The autotuner: times the batch's first `sample` models (full runs) under each candidate of
-// workers x blocks per launch and returns the fastest, by phonon-steps per second.
+// The autotuner: times the batch's first `sample` models (full runs) under each candidate and
+// returns the fastest, by phonon-steps per second: batched launches with 4, 8, 16 or 32 phonons
+// per thread in a work item, and models on their own under workers {4, 8, 16, 32} x blocks per
+// launch {1/8, 1/4, 1/2, 1} of the multiprocessors.
 BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, double* best_rate);
 
 }// namespace psim

@@ -525,53 +525,67 @@ gpu::InterpDesc HostModel::interp_desc(double eff) const {
 // reference's stability check stores every sensor's mean temperature as its steady temperature
 // (model.cpp:250-272, sensorController.cpp:57-62) and the energy per phonon is recomputed from
 // it before the results are scaled (model.cpp:171); with MAX_ITERS = 1 no re-run follows.
-void HostModel::run() {
-    const auto t0 = std::chrono::steady_clock::now();
+void HostModel::begin_runs() {
+    run_t0_ = std::chrono::steady_clock::now();
     if (stop_on_ && (num_runs_ != 1 || type_ == SimType::SteadyState)) {
         throw std::invalid_argument("stopping at steady state needs a single-run periodic or transient model");
     }
     runs_.clear();
     recorded_ = desc_.recorded;
-    for (std::size_t run = 0; run < num_runs_; ++run) {
-        const auto [mn, mx] = bounds();
-        build_tables(mn, mx);
+}
+
+void HostModel::prepare_run(std::size_t run) {
+    const auto [mn, mx] = bounds();
+    build_tables(mn, mx);
+    eff_energy_ = total_energy() / static_cast<double>(num_phonons_);
+    const bool fresh = !engine_;
+    if (fresh) { engine_ = std::make_unique<gpu::Engine>(desc_); }
+    engine_->reset();
+    if (fresh) { engine_->add_h2d(engine_->model_bytes()); }
+    const std::vector<double> cell_energy = cell_energies();
+    const std::vector<double> emit_energy = emit_energies();
+    const std::vector<double> sensor_t0 = sensor_init_temps();
+    const std::uint64_t run_seed = seed_ * 0x9E3779B97F4A7C15ULL + run * 0xD1B54A32D192ED03ULL + 1;
+    engine_->init_builders(t_eq_, eff_energy_, cell_energy.data(), emit_energy.data(), sensor_t0.data(), run_seed);
+    engine_->set_steady_stop(stop_on_, stop_crit_, stop_check_);
+    engine_->set_grid(grid_);
+}
+
+void HostModel::finish_run() {
+    recorded_ = std::min<std::size_t>(desc_.recorded, engine_->steps_run());
+    if (type_ == SimType::SteadyState) {
+        std::vector<double> finals(sensors_.size());
+        engine_->final_temps(interp_desc(eff_energy_), start_step_, finals.data());
+        for (std::size_t s = 0; s < sensors_.size(); ++s) { sensors_[s].t_steady = finals[s]; }
         eff_energy_ = total_energy() / static_cast<double>(num_phonons_);
-        const bool fresh = !engine_;
-        if (fresh) { engine_ = std::make_unique<gpu::Engine>(desc_); }
-        engine_->reset();
-        if (fresh) { engine_->add_h2d(engine_->model_bytes()); }
-        const std::vector<double> cell_energy = cell_energies();
-        const std::vector<double> emit_energy = emit_energies();
-        const std::vector<double> sensor_t0 = sensor_init_temps();
-        const std::uint64_t run_seed = seed_ * 0x9E3779B97F4A7C15ULL + run * 0xD1B54A32D192ED03ULL + 1;
-        engine_->init_builders(t_eq_, eff_energy_, cell_energy.data(), emit_energy.data(), sensor_t0.data(), run_seed);
-        engine_->set_steady_stop(stop_on_, stop_crit_, stop_check_);
-        engine_->set_grid(grid_);
-        engine_->run(precision_, stream_);
-        recorded_ = std::min<std::size_t>(desc_.recorded, engine_->steps_run());
-        if (type_ == SimType::SteadyState) {
-            std::vector<double> finals(sensors_.size());
-            engine_->final_temps(interp_desc(eff_energy_), start_step_, finals.data());
-            for (std::size_t s = 0; s < sensors_.size(); ++s) { sensors_[s].t_steady = finals[s]; }
-            eff_energy_ = total_energy() / static_cast<double>(num_phonons_);
-        }
-        std::vector<Measurement> ms(sensors_.size());
-        std::vector<double> temps(sensors_.size() * recorded_);
-        std::vector<double> fluxes(sensors_.size() * recorded_ * 2);
-        std::vector<double> stats(sensors_.size() * 6);
-        engine_->interpret(interp_desc(eff_energy_), temps.data(), fluxes.data(), stats.data());
-        for (std::size_t s = 0; s < sensors_.size(); ++s) {
-            Measurement& m = ms[s];
-            m.id = sensors_[s].id;
-            std::copy(stats.begin() + static_cast<std::ptrdiff_t>(6 * s), stats.begin() + static_cast<std::ptrdiff_t>(6 * s + 6), m.stats.begin());
-            m.temps.assign(temps.begin() + static_cast<std::ptrdiff_t>(s * recorded_), temps.begin() + static_cast<std::ptrdiff_t>((s + 1) * recorded_));
-            m.fluxes.assign(fluxes.begin() + static_cast<std::ptrdiff_t>(2 * s * recorded_), fluxes.begin() + static_cast<std::ptrdiff_t>(2 * (s + 1) * recorded_));
-        }
-        std::sort(ms.begin(), ms.end(), [](const Measurement& a, const Measurement& b) { return a.id < b.id; });
-        runs_.push_back(std::move(ms));
-        for (auto& s : sensors_) { s.t_steady = s.t_init; }// Model::reset(true) before the next run
     }
-    last_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::vector<Measurement> ms(sensors_.size());
+    std::vector<double> temps(sensors_.size() * recorded_);
+    std::vector<double> fluxes(sensors_.size() * recorded_ * 2);
+    std::vector<double> stats(sensors_.size() * 6);
+    engine_->interpret(interp_desc(eff_energy_), temps.data(), fluxes.data(), stats.data());
+    for (std::size_t s = 0; s < sensors_.size(); ++s) {
+        Measurement& m = ms[s];
+        m.id = sensors_[s].id;
+        std::copy(stats.begin() + static_cast<std::ptrdiff_t>(6 * s), stats.begin() + static_cast<std::ptrdiff_t>(6 * s + 6), m.stats.begin());
+        m.temps.assign(temps.begin() + static_cast<std::ptrdiff_t>(s * recorded_), temps.begin() + static_cast<std::ptrdiff_t>((s + 1) * recorded_));
+        m.fluxes.assign(fluxes.begin() + static_cast<std::ptrdiff_t>(2 * s * recorded_), fluxes.begin() + static_cast<std::ptrdiff_t>(2 * (s + 1) * recorded_));
+    }
+    std::sort(ms.begin(), ms.end(), [](const Measurement& a, const Measurement& b) { return a.id < b.id; });
+    runs_.push_back(std::move(ms));
+    for (auto& s : sensors_) { s.t_steady = s.t_init; }// Model::reset(true) before the next run
+}
+
+void HostModel::end_runs() { last_seconds_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - run_t0_).count(); }
+
+void HostModel::run() {
+    begin_runs();
+    for (std::size_t run = 0; run < num_runs_; ++run) {
+        prepare_run(run);
+        engine_->run(precision_, stream_);
+        finish_run();
+    }
+    end_runs();
 }
 
 std::vector<double> HostModel::cell_energies() const {

@@ -7,6 +7,7 @@
 #pragma once
 
 #include <array>
+#include <chrono>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -97,6 +98,15 @@ public:
     void set_start_temps(const std::vector<double>& temps);
     std::vector<double> start_temps() const;
     void run();// Model::runSimulation
+    // run() in parts, for transports run elsewhere (a batch): begin_runs(), then per run r
+    // prepare_run(r) (tables, engine, phonon builders), the engine's transport, finish_run()
+    // (interpretation and results); end_runs() at the end.
+    void begin_runs();
+    void prepare_run(std::size_t run);
+    void finish_run();
+    void end_runs();
+    int precision() const noexcept { return precision_; }
+    bool steady_stop() const noexcept { return stop_on_; }
     void export_results(const std::string& json_path, double seconds) const;
 
     std::size_t n_sensors() const noexcept { return sensors_.size(); }
@@ -158,6 +168,7 @@ private:
     std::unique_ptr<gpu::Engine> engine_;
     std::vector<std::vector<Measurement>> runs_;
     double last_seconds_{ 0. };
+    std::chrono::steady_clock::time_point run_t0_{};
 
     // assembly
     void set_type(SimType t, std::size_t interval);

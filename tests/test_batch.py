@@ -1,5 +1,6 @@
 """Many models on one GPU (psim_batch_run / psim_batch_autotune): each model's results equal
-those of the same model run alone, whatever runs beside it, the stream or the grid."""
+those of the same model run alone, whatever runs beside it, the stream or the grid, in the
+batched launches fed by a device work queue as on worker threads."""
 import numpy as np
 import pytest
 
@@ -28,12 +29,18 @@ def test_batch_fails_loudly_without_a_device(built):
 
 
 CASES = [("bar_ss", 3, 0), ("kinked_small", 4, 0), ("plate_small", 5, 0), ("bar_periodic", 6, 0),
-         ("bar_full", 7, 0), ("bar_phasor", 8, 0), ("kinked_small", 9, 1), ("bar_ss", 10, 0)]
+         ("bar_full", 7, 0), ("bar_phasor", 8, 0), ("kinked_small", 9, 1), ("bar_ss", 10, 0), ("bar_runs", 11, 0),
+         ("kinked_small", 12, 0), ("plate_small", 13, 0)]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("workers,max_blocks", [(3, 8), (8, 0)])
-def test_batch_results_equal_single_runs(gpu, workers, max_blocks):
+@pytest.mark.parametrize("workers,max_blocks,queue,per_thread", [(3, 8, False, 16), (8, 0, False, 16), (4, 0, True, 16),
+                                                                 (8, 0, True, 1), (2, 0, True, 64)])
+def test_batch_results_equal_single_runs(gpu, workers, max_blocks, queue, per_thread):
+    """Models of several step counts, modes and precisions: steady state, full, periodic,
+    transient, phasor, three averaged runs, and an FP64 model (which runs on its own).  With the
+    device queue the FP32 models of each step count share launches; work items of 1, 16 and 64
+    phonons per thread cut the models' phonons at different places."""
     from psim_gb300 import api
     alone = []
     for name, seed, prec in CASES:
@@ -41,7 +48,7 @@ def test_batch_results_equal_single_runs(gpu, workers, max_blocks):
         m.run(seed=seed, precision=prec)
         alone.append((m.tallies(), m.measurements()))
     models = [api.Model(model_path(name)).set_options(seed=seed, precision=prec) for name, seed, prec in CASES]
-    secs, steps = api.batch_run(models, workers=workers, max_blocks=max_blocks)
+    secs, steps = api.batch_run(models, workers=workers, max_blocks=max_blocks, device_queue=queue, per_thread=per_thread)
     assert secs > 0 and steps > 0
     total = 0
     for m, ((e, f), st) in zip(models, alone):
@@ -57,6 +64,8 @@ def test_batch_autotune_picks_valid_options(gpu):
     from psim_gb300 import api
     models = [api.Model(model_path("bar_periodic")).set_options(seed=s) for s in range(1, 5)]
     opt, rate = api.batch_autotune(models, sample=4)
-    assert opt.workers in (4, 8, 16, 32) and opt.max_blocks >= 1 and rate > 0
-    secs, steps = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks)
+    assert opt.workers in (4, 8, 16, 32) and rate > 0
+    assert (opt.device_queue == 1 and opt.per_thread in (4, 8, 16, 32)) or (opt.device_queue == 0 and opt.max_blocks >= 1)
+    secs, steps = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks, device_queue=bool(opt.device_queue),
+                                per_thread=opt.per_thread)
     assert steps > 0

@@ -61,17 +61,24 @@ def test_steps_per_launch_do_not_change_results(api, monkeypatch, tmp_path, name
     boundaries in registers; plain boundaries are crossed in a warp-uniform loop while enough
     lanes cross one.  Tallies, the population history and the phonon-step count equal those of
     one step per launch, with every table in shared memory, with the tables but not the cell
-    records there, and with global ones, and whatever the coasting threshold.  plate_2560 has
+    records there, and with global ones, whatever the coasting threshold, with survivors written
+    in two groups by their time to scattering or their velocity, and in a chunked run whose state
+    buffers grow between chunks of launches (both groups copied).  plate_2560 has
     more sensors than the shared-memory tally holds (tallies in global memory)."""
     from psim_gb300 import modelgen as mg
     path = (mg.write(mg.plate(nx=64, ny=40, num_phonons=30000, num_measurements=120, sim_time=0.12),
                      os.path.join(str(tmp_path), "plate_2560.json")) if name == "plate_2560" else model_path(name))
     ref = None
-    for stage, fuse, coast in (("1", "1", "0"), ("1", "3", "16"), ("1", "8", "1"), ("1", "16", "32"), ("0", "5", "16"),
-                               ("2", "7", "16"), ("2", "2", "0")):
+    # (staging, steps per launch, coasting lanes, survivor grouping, chunked run with growing buffers)
+    for stage, fuse, coast, sort, chunked in (("1", "1", "0", "0", "0"), ("1", "3", "16", "0", "0"), ("1", "8", "1", "0", "0"),
+                                              ("1", "16", "32", "0", "0"), ("0", "5", "16", "0", "0"), ("2", "7", "16", "0", "0"),
+                                              ("2", "2", "0", "0", "0"), ("1", "8", "0", "1:9", "0"), ("1", "6", "0", "2:5000", "1"),
+                                              ("1", "4", "0", "1:4", "1")):
         monkeypatch.setenv("PSIM_GB300_STAGE", stage)
         monkeypatch.setenv("PSIM_GB300_FUSE", fuse)
         monkeypatch.setenv("PSIM_GB300_COAST", coast)
+        monkeypatch.setenv("PSIM_GB300_SORT", sort)
+        monkeypatch.setenv("PSIM_GB300_CHUNKED", chunked)
         m = api.Model(path)
         m.run(seed=11)
         e, f = m.tallies()
@@ -88,6 +95,8 @@ def test_steps_per_launch_do_not_change_results(api, monkeypatch, tmp_path, name
     monkeypatch.delenv("PSIM_GB300_STAGE")
     monkeypatch.delenv("PSIM_GB300_FUSE")
     monkeypatch.delenv("PSIM_GB300_COAST")
+    monkeypatch.delenv("PSIM_GB300_SORT")
+    monkeypatch.delenv("PSIM_GB300_CHUNKED")
 
 
 def test_counters_and_phonon_steps(api):

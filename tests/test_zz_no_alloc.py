@@ -75,6 +75,23 @@ def test_rejects_inputs_beyond_the_scratch(env):
     with pytest.raises(api.PsimError) as exc:
         api.final_temps_noalloc(d, big.data_ptr(), 0, out.data_ptr(), None)
     assert exc.value.code == 4 and "scratch" in str(exc.value)
+    # a rejected call enqueues nothing: a valid call pending on a stream keeps its scratch and result,
+    # and the rejected call's output buffer keeps its contents
+    m_ok, d_ok, counts = _case(api, "bar_ss")
+    want = api.final_temps(d_ok, counts, 1)
+    e_ok = torch.from_numpy(counts).cuda()
+    out_ok = torch.full((S,), float("nan"), dtype=torch.float64, device="cuda")
+    sentinel = torch.full((S,), -12345.0, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    api.final_temps_noalloc(d_ok, e_ok.data_ptr(), 1, out_ok.data_ptr(), stream.cuda_stream)
+    with pytest.raises(api.PsimError) as exc:
+        api.final_temps_noalloc(d, big.data_ptr(), 0, sentinel.data_ptr(), stream.cuda_stream)
+    assert exc.value.code == 4
+    stream.synchronize()
+    assert np.array_equal(out_ok.cpu().numpy(), want)
+    assert bool((sentinel == -12345.0).all())
+    m_ok.close()
     # past the start step is an argument error, not a size error
     with pytest.raises(api.PsimError) as exc:
         api.final_temps_noalloc(d, big.data_ptr(), K + 1, out.data_ptr(), None)
