@@ -299,22 +299,25 @@ int psim_final_temps(const psim_interp_desc* d, const int64_t* energy, uint64_t 
  * count and flux components are cut into windows of `window` steps, each window into `batches`
  * equal batches; a window's standard error is the spread of its batch means over sqrt(batches)
  * (per-step tallies are correlated: a phonon stays in a sensor's cells for several steps); a
- * window agrees with the previous one when every mean differs by at most z combined standard
+ * window agrees with an anchor window when every mean differs by at most z combined standard
  * errors; a sensor is steady from window j when the `patience` windows after j all agree with
- * their predecessors; the onset is the largest over the sensors, in steps (-1: not steady).
- * Evaluated by a GPU kernel on the exact integer tallies.  window must be a multiple of
- * batches, batches >= 2, z > 0, patience >= 1 (PSIM_ERR_INVALID otherwise).
+ * window j (a window that disagrees becomes the next anchor) and, with drift_z > 0, the least-
+ * squares slope of each quantity's means over those patience + 1 windows lies within drift_z of
+ * its standard error (a slope beyond it also makes the latest window the anchor); the onset is
+ * the largest over the sensors, in steps (-1: not steady).  Evaluated by a GPU kernel on the
+ * exact integer tallies.  window must be a multiple of batches, batches >= 2, z > 0,
+ * patience >= 1, drift_z >= 0 (PSIM_ERR_INVALID otherwise).
  * ------------------------------------------------------------------------------------------ */
 /* On raw tallies energy[S][K] and flux[S][K][2] (as psim_sim_tallies returns them); flux is taken
  * at 2^-20 m/s resolution.  per_sensor[S] may be NULL. */
 int psim_steady_state(const int64_t* energy, const double* flux, uint32_t n_sensors, uint64_t recorded_steps,
-                      uint32_t window, uint32_t batches, double z, uint32_t patience, int64_t* onset_step,
-                      int64_t* per_sensor);
+                      uint32_t window, uint32_t batches, double z, uint32_t patience, double drift_z,
+                      int64_t* onset_step, int64_t* per_sensor);
 /* On the recorded steps of the simulator's / model's last run (its tallies stay on the GPU). */
 int psim_sim_steady_state(const psim_sim* s, uint32_t window, uint32_t batches, double z, uint32_t patience,
-                          int64_t* onset_step, int64_t* per_sensor);
+                          double drift_z, int64_t* onset_step, int64_t* per_sensor);
 int psim_model_steady_state(const psim_model* m, uint32_t window, uint32_t batches, double z, uint32_t patience,
-                            int64_t* onset_step, int64_t* per_sensor);
+                            double drift_z, int64_t* onset_step, int64_t* per_sensor);
 /* Stop later runs once their recorded steps are steady by the criterion above, checked every
  * check_every steps (0: every (patience + 1) x window steps) between launches; enable = 0 turns
  * it off.  Only for runs that record every step: a single-run periodic or transient model, or a
@@ -322,9 +325,9 @@ int psim_model_steady_state(const psim_model* m, uint32_t window, uint32_t batch
  * results of a stopped run cover the steps it simulated: psim_model_shape reports them as the
  * recorded steps, and psim_model_series / psim_model_tallies return that many. */
 int psim_model_set_steady_stop(psim_model* m, int32_t enable, uint32_t window, uint32_t batches, double z,
-                               uint32_t patience, uint64_t check_every);
+                               uint32_t patience, double drift_z, uint64_t check_every);
 int psim_sim_set_steady_stop(psim_sim* s, int32_t enable, uint32_t window, uint32_t batches, double z,
-                             uint32_t patience, uint64_t check_every);
+                             uint32_t patience, double drift_z, uint64_t check_every);
 /* Measurement steps the last run simulated. */
 int psim_model_steps_run(const psim_model* m, uint64_t* steps);
 int psim_sim_steps_run(const psim_sim* s, uint64_t* steps);

@@ -122,15 +122,15 @@ SIGNATURES = {
                                                 ctypes.c_void_p, ctypes.c_void_p]),
     "psim_final_temps_noalloc_max_bytes": (ctypes.c_uint64, []),
     "psim_steady_state": (ctypes.c_int, [_c_i64p, _c_dp, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32,
-                                         ctypes.c_double, ctypes.c_uint32, _c_i64p, _c_i64p]),
+                                         ctypes.c_double, ctypes.c_uint32, ctypes.c_double, _c_i64p, _c_i64p]),
     "psim_sim_steady_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_uint32,
-                                             _c_i64p, _c_i64p]),
+                                             ctypes.c_double, _c_i64p, _c_i64p]),
     "psim_model_steady_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double,
-                                               ctypes.c_uint32, _c_i64p, _c_i64p]),
+                                               ctypes.c_uint32, ctypes.c_double, _c_i64p, _c_i64p]),
     "psim_model_set_steady_stop": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
-                                                  ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64]),
+                                                  ctypes.c_double, ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64]),
     "psim_sim_set_steady_stop": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint32,
-                                                ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64]),
+                                                ctypes.c_double, ctypes.c_uint32, ctypes.c_double, ctypes.c_uint64]),
     "psim_model_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
     "psim_sim_steps_run": (ctypes.c_int, [ctypes.c_void_p, _c_u64p]),
     "psim_batch_run": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.POINTER(BatchOptions),
@@ -245,9 +245,10 @@ class Model:
         return self
 
     def set_steady_stop(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3, check_every: int = 0,
+                        drift_z: float = 0.0,
                         enable: bool = True) -> None:
         """Stop later runs at steady state (single-run periodic or transient models)."""
-        _check(lib().psim_model_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, check_every))
+        _check(lib().psim_model_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, drift_z, check_every))
 
     def steps_run(self) -> int:
         out = ctypes.c_uint64()
@@ -314,9 +315,10 @@ class Model:
         _check(lib().psim_model_sim_desc(self._h, ctypes.byref(d)))
         return d
 
-    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3) -> Tuple[int, np.ndarray]:
+    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3,
+                     drift_z: float = 0.0) -> Tuple[int, np.ndarray]:
         """Steady-state onset (step, -1 if none) and per-sensor onsets over the last run."""
-        return _steady(lib().psim_model_steady_state, self._h, self.n_sensors, window, batches, z, patience)
+        return _steady(lib().psim_model_steady_state, self._h, self.n_sensors, window, batches, z, patience, drift_z)
 
     def interp_desc(self, eff_energy: float = 0.0) -> InterpDesc:
         d = InterpDesc()
@@ -374,12 +376,14 @@ class Simulator:
         _check(lib().psim_sim_tallies(self._h, _i64(energy), _dp(flux)))
         return energy, flux
 
-    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3) -> Tuple[int, np.ndarray]:
-        return _steady(lib().psim_sim_steady_state, self._h, self.desc.n_sensors, window, batches, z, patience)
+    def steady_state(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3,
+                     drift_z: float = 0.0) -> Tuple[int, np.ndarray]:
+        return _steady(lib().psim_sim_steady_state, self._h, self.desc.n_sensors, window, batches, z, patience, drift_z)
 
     def set_steady_stop(self, window: int = 250, batches: int = 5, z: float = 3.0, patience: int = 3, check_every: int = 0,
+                        drift_z: float = 0.0,
                         enable: bool = True) -> None:
-        _check(lib().psim_sim_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, check_every))
+        _check(lib().psim_sim_set_steady_stop(self._h, 1 if enable else 0, window, batches, z, patience, drift_z, check_every))
 
     def steps_run(self) -> int:
         out = ctypes.c_uint64()
@@ -503,15 +507,16 @@ def batch_autotune(models, sample: int = 16) -> Tuple[BatchOptions, float]:
     return opt, float(rate.value)
 
 
-def _steady(fn, handle, n_sensors: int, window: int, batches: int, z: float, patience: int) -> Tuple[int, np.ndarray]:
+def _steady(fn, handle, n_sensors: int, window: int, batches: int, z: float, patience: int,
+            drift_z: float = 0.0) -> Tuple[int, np.ndarray]:
     onset = ctypes.c_int64()
     per = np.zeros(n_sensors, dtype=np.int64)
-    _check(fn(handle, window, batches, z, patience, ctypes.byref(onset), _i64(per)))
+    _check(fn(handle, window, batches, z, patience, drift_z, ctypes.byref(onset), _i64(per)))
     return int(onset.value), per
 
 
 def steady_state(energy: np.ndarray, flux: np.ndarray, window: int = 250, batches: int = 5, z: float = 3.0,
-                 patience: int = 3) -> Tuple[int, np.ndarray]:
+                 patience: int = 3, drift_z: float = 0.0) -> Tuple[int, np.ndarray]:
     """psim_steady_state on raw tallies energy [S,K] and flux [S,K,2]: (onset step or -1, per-sensor onsets)."""
     energy = np.ascontiguousarray(energy, dtype=np.int64)
     flux = np.ascontiguousarray(flux, dtype=np.float64)
@@ -519,7 +524,7 @@ def steady_state(energy: np.ndarray, flux: np.ndarray, window: int = 250, batche
     assert flux.shape == (S, K, 2)
     onset = ctypes.c_int64()
     per = np.zeros(S, dtype=np.int64)
-    _check(lib().psim_steady_state(_i64(energy), _dp(flux), S, K, window, batches, z, patience, ctypes.byref(onset),
+    _check(lib().psim_steady_state(_i64(energy), _dp(flux), S, K, window, batches, z, patience, drift_z, ctypes.byref(onset),
                                    _i64(per)))
     return int(onset.value), per
 

@@ -419,61 +419,66 @@ int psim_final_temps(const psim_interp_desc* d, const int64_t* energy, uint64_t 
 
 // ------------------------------------------------------------------ steady-state detection
 namespace {
-psim::gpu::SteadyCriterion criterion(uint32_t window, uint32_t batches, double z, uint32_t patience) {
+psim::gpu::SteadyCriterion criterion(uint32_t window, uint32_t batches, double z, uint32_t patience, double drift_z) {
     psim::gpu::SteadyCriterion c;
     c.window = window;
     c.batches = batches;
     c.z = z;
     c.patience = patience;
+    c.drift_z = drift_z;
     psim::gpu::validate_steady(c);
     return c;
 }
 }// namespace
 
 int psim_steady_state(const int64_t* energy, const double* flux, uint32_t n_sensors, uint64_t recorded_steps, uint32_t window,
-                      uint32_t batches, double z, uint32_t patience, int64_t* onset_step, int64_t* per_sensor) {
+                      uint32_t batches, double z, uint32_t patience, double drift_z, int64_t* onset_step, int64_t* per_sensor) {
     if (onset_step == nullptr || (n_sensors > 0 && recorded_steps > 0 && (energy == nullptr || flux == nullptr))) {
         return fail(PSIM_ERR_INVALID, "null argument");
     }
     return guard([&]() {
-        const auto c = criterion(window, batches, z, patience);
+        const auto c = criterion(window, batches, z, patience, drift_z);
         *onset_step = psim::gpu::steady_onset_host(energy, flux, n_sensors, recorded_steps, c, reinterpret_cast<long long*>(per_sensor));
     });
 }
 
-int psim_sim_steady_state(const psim_sim* s, uint32_t window, uint32_t batches, double z, uint32_t patience, int64_t* onset_step,
+int psim_sim_steady_state(const psim_sim* s, uint32_t window, uint32_t batches, double z, uint32_t patience, double drift_z,
+                          int64_t* onset_step,
                           int64_t* per_sensor) {
     if (s == nullptr || onset_step == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     return guard([&]() {
-        *onset_step = s->e->steady_onset(criterion(window, batches, z, patience), reinterpret_cast<long long*>(per_sensor));
+        *onset_step = s->e->steady_onset(criterion(window, batches, z, patience, drift_z), reinterpret_cast<long long*>(per_sensor));
     });
 }
 
-int psim_model_steady_state(const psim_model* m, uint32_t window, uint32_t batches, double z, uint32_t patience,
+int psim_model_steady_state(const psim_model* m, uint32_t window, uint32_t batches, double z, uint32_t patience, double drift_z,
                             int64_t* onset_step, int64_t* per_sensor) {
     if (m == nullptr || onset_step == nullptr) { return fail(PSIM_ERR_INVALID, "null argument"); }
     if (m->m->engine() == nullptr) { return fail(PSIM_ERR_INVALID, "the model has not been run"); }
     return guard([&]() {
-        *onset_step = m->m->engine()->steady_onset(criterion(window, batches, z, patience), reinterpret_cast<long long*>(per_sensor));
+        *onset_step = m->m->engine()->steady_onset(criterion(window, batches, z, patience, drift_z),
+                                                   reinterpret_cast<long long*>(per_sensor));
     });
 }
 
 int psim_model_set_steady_stop(psim_model* m, int32_t enable, uint32_t window, uint32_t batches, double z, uint32_t patience,
+                               double drift_z,
                                uint64_t check_every) {
     if (m == nullptr) { return fail(PSIM_ERR_INVALID, "null model"); }
     return guard([&]() {
         psim::gpu::SteadyCriterion c;
-        if (enable != 0) { c = criterion(window, batches, z, patience); }
+        if (enable != 0) { c = criterion(window, batches, z, patience, drift_z); }
         m->m->set_steady_stop(enable != 0, c, check_every);
     });
 }
 
 int psim_sim_set_steady_stop(psim_sim* s, int32_t enable, uint32_t window, uint32_t batches, double z, uint32_t patience,
+                             double drift_z,
                              uint64_t check_every) {
     if (s == nullptr) { return fail(PSIM_ERR_INVALID, "null simulator"); }
     return guard([&]() {
         psim::gpu::SteadyCriterion c;
-        if (enable != 0) { c = criterion(window, batches, z, patience); }
+        if (enable != 0) { c = criterion(window, batches, z, patience, drift_z); }
         s->e->set_steady_stop(enable != 0, c, check_every);
     });
 }

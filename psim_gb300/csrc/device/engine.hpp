@@ -81,6 +81,7 @@ struct SteadyCriterion {
     std::uint32_t batches{ 5 };  // batch means per window (window is a multiple of it)
     double z{ 3. };              // agreement tolerance in combined standard errors
     std::uint32_t patience{ 3 }; // consecutive agreeing windows
+    double drift_z{ 0. };        // trend test over the anchor and its agreeing windows (0: none)
 };
 
 class Engine {

@@ -14,6 +14,12 @@
 //     itself (the anchor: a drift too slow to show between neighbouring windows still has to stay
 //     within the tolerance over all M of them); a window that disagrees becomes the next anchor;
 //     the onset is step j*W;
+//   - with a trend tolerance zd > 0, the M + 1 windows from the anchor must also show no linear
+//     trend: the least-squares slope of each quantity's window means over the window index
+//     (weighted equally, its variance from the windows' standard errors) must lie within zd of its
+//     standard error; a trend makes the latest window the next anchor, like a disagreement.  A
+//     relaxation slow enough to stay within z standard errors of the anchor for M windows still
+//     shows as a consistent slope;
 //   - the model is steady at the largest onset over its sensors, and not steady while any
 //     sensor has none.
 // The statistics are computed in FP64 from the exact integer tallies (flux in fixed point), in a
@@ -45,7 +51,7 @@ struct WindowStats {
 
 // One warp per sensor: lanes split each batch's steps, then reduce.
 __global__ void steady_kernel(const TallySlot* tally, std::uint32_t S, std::uint64_t k_used, std::uint32_t W, std::uint32_t B,
-                              double z, std::uint32_t M, long long* onset) {
+                              double z, std::uint32_t M, double zd, long long* onset) {
     const std::uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31U;
     if (warp >= S) { return; }
@@ -56,6 +62,12 @@ __global__ void steady_kernel(const TallySlot* tally, std::uint32_t S, std::uint
     WindowStats anchor{};
     std::uint64_t anchor_w = 0;
     std::uint32_t streak = 0;
+    // sums over the windows from the anchor (index i = 0, 1, ...) for the trend test: sum i,
+    // sum i^2, and per quantity sum d, sum i d (d: window mean minus the anchor's) and sum se^2,
+    // sum i se^2, sum i^2 se^2
+    double n_w = 0., s_i = 0., s_ii = 0.;
+    double s_d[3] = { 0., 0., 0. }, s_id[3] = { 0., 0., 0. };
+    double v0[3] = { 0., 0., 0. }, v1[3] = { 0., 0., 0. }, v2[3] = { 0., 0., 0. };
     long long result = -1;
     for (std::uint64_t w = 0; w < nw && result < 0; ++w) {
         double bsum[3] = { 0., 0., 0. };// batch means about 'shift'
@@ -94,12 +106,57 @@ __global__ void steady_kernel(const TallySlot* tally, std::uint32_t S, std::uint
             const double tol = z * sqrt(cur.se[q] * cur.se[q] + anchor.se[q] * anchor.se[q]);
             agree = agree && fabs(cur.mean[q] - anchor.mean[q]) <= tol;
         }
+        bool reset = !agree;
         if (agree) {
-            if (++streak >= M) { result = static_cast<long long>(anchor_w * W); }
-        } else {
+            ++streak;
+            const double i = static_cast<double>(streak);
+            n_w += 1.;
+            s_i += i;
+            s_ii += i * i;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const double d = cur.mean[q] - anchor.mean[q];
+                const double v = cur.se[q] * cur.se[q];
+                s_d[q] += d;
+                s_id[q] += i * d;
+                v0[q] += v;
+                v1[q] += i * v;
+                v2[q] += i * i * v;
+            }
+            if (streak >= M) {
+                bool flat = true;
+                if (zd > 0.) {
+                    const double ib = s_i / n_w;
+                    const double sxx = s_ii - n_w * ib * ib;
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        const double slope = (s_id[q] - ib * s_d[q]) / sxx;
+                        const double var = fmax(0., v2[q] - 2. * ib * v1[q] + ib * ib * v0[q]) / (sxx * sxx);
+                        flat = flat && fabs(slope) <= zd * sqrt(var);
+                    }
+                }
+                if (flat) {
+                    result = static_cast<long long>(anchor_w * W);
+                } else {
+                    reset = true;
+                }
+            }
+        }
+        if (reset) {
             anchor = cur;
             anchor_w = w;
             streak = 0;
+            n_w = 1.;
+            s_i = 0.;
+            s_ii = 0.;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                s_d[q] = 0.;
+                s_id[q] = 0.;
+                v0[q] = cur.se[q] * cur.se[q];
+                v1[q] = 0.;
+                v2[q] = 0.;
+            }
         }
         prev = cur;
     }
@@ -133,6 +190,7 @@ void validate_steady(const SteadyCriterion& c) {
     }
     if (!(c.z > 0.)) { throw std::invalid_argument("steady-state tolerance must be positive"); }
     if (c.patience < 1) { throw std::invalid_argument("steady-state patience must be at least 1 window"); }
+    if (!(c.drift_z >= 0.) || !std::isfinite(c.drift_z)) { throw std::invalid_argument("steady-state trend tolerance must be finite and not negative"); }
 }
 
 long long steady_onset_device(const void* tally, std::uint32_t S, std::uint64_t k_used, const SteadyCriterion& c,
@@ -145,7 +203,7 @@ long long steady_onset_device(const void* tally, std::uint32_t S, std::uint64_t 
         const unsigned threads = 256;
         const unsigned blocks = static_cast<unsigned>((static_cast<std::uint64_t>(S) * 32 + threads - 1) / threads);
         steady_kernel<<<blocks, threads, 0, stream>>>(static_cast<const TallySlot*>(tally), S, k_used, c.window, c.batches,
-                                                      c.z, c.patience, static_cast<long long*>(d_onset.p));
+                                                      c.z, c.patience, c.drift_z, static_cast<long long*>(d_onset.p));
         check(cudaGetLastError(), "steady-state kernel");
         check(cudaMemcpyAsync(onset.data(), d_onset.p, S * sizeof(long long), cudaMemcpyDeviceToHost, stream), "copy onsets");
         check(cudaStreamSynchronize(stream), "steady-state sync");

@@ -68,6 +68,12 @@ def _models(seeds: Sequence[int], td: str, *, periodic: bool, steps: int, scale:
 
 CHUNK = 128  # models alive at once: each keeps GPU buffers sized for its run's phonons
 
+# The steady stop of the evaluation's runs: agreement with the anchor window at STOP_Z standard
+# errors for STOP_PATIENCE windows, and (STOP_DRIFT_Z > 0) no trend over them beyond STOP_DRIFT_Z.
+STOP_Z = 3.0
+STOP_PATIENCE = 3
+STOP_DRIFT_Z = 0.0
+
 
 def generate(seeds: Sequence[int], *, steps: int = 3000, scale: float = 1.0, workers: int = 16) -> Tuple[np.ndarray, np.ndarray]:
     """Steady fields of the rectangles drawn from ``seeds``: the Monte Carlo run of each (steady
@@ -146,7 +152,7 @@ def onset_vs_reference(temps: np.ndarray, t_inf: np.ndarray, spread: np.ndarray,
 
 
 def stopped_within(m: api.Model, ref: Tuple[np.ndarray, np.ndarray, int], window: int, batches: int,
-                   patience: int) -> Tuple[bool, bool]:
+                   patience: int, z: float = 3.0, drift_z: float = 0.0) -> Tuple[bool, bool]:
     """Whether a run stopped by the steady-state detector was steady at 3 SE where the detector
     said so, by two standards:
     - windows: every window mean of every sensor from the detector's onset to the stop lies
@@ -156,7 +162,7 @@ def stopped_within(m: api.Model, ref: Tuple[np.ndarray, np.ndarray, int], window
       length (spread x sqrt(window / steps), windows taken as independent), family-wise over the
       sensors: a much tighter standard, since the mean of many windows has a smaller error."""
     temps, _ = m.series(0)
-    onset, _ = m.steady_state(window=window, batches=batches, patience=patience)
+    onset, _ = m.steady_state(window=window, batches=batches, z=z, patience=patience, drift_z=drift_z)
     k = temps.shape[1]
     start = onset if 0 <= onset < k else max(k - window, 0)
     t_inf, spread, dof = ref
@@ -169,7 +175,8 @@ def stopped_within(m: api.Model, ref: Tuple[np.ndarray, np.ndarray, int], window
 
 
 def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: float = 1.0, window: int = 100,
-             batches: int = 5, patience: int = 3, workers: int = 16) -> Dict:
+             batches: int = 5, patience: int = STOP_PATIENCE, z: float = STOP_Z, drift_z: float = STOP_DRIFT_Z,
+             workers: int = 16) -> Dict:
     """Cold and warm starts of the rectangles drawn from ``seeds``.
 
     A third, twice as long, warm-started run of each rectangle with its own seed gives the steady
@@ -212,12 +219,14 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
                 t_inf = ref_k[0]
                 rows.append({"cold": onset_vs_reference(tc, *ref_k, window),
                              "warm": onset_vs_reference(tw, *ref_k, window),
-                             "cold_detector": mc.steady_state(window=window, batches=batches, patience=patience)[0],
-                             "warm_detector": mw.steady_state(window=window, batches=batches, patience=patience)[0],
+                             "cold_detector": mc.steady_state(window=window, batches=batches, z=z, patience=patience,
+                                                              drift_z=drift_z)[0],
+                             "warm_detector": mw.steady_state(window=window, batches=batches, z=z, patience=patience,
+                                                              drift_z=drift_z)[0],
                              "start_error_K": float(np.sqrt(np.mean((tw[:, 0] - t_inf) ** 2))),
                              "cold_start_error_K": float(np.sqrt(np.mean((tc[:, 0] - t_inf) ** 2)))})
             for m, _ in cold + warm:
-                m.set_steady_stop(window=window, batches=batches, patience=patience)
+                m.set_steady_stop(window=window, batches=batches, z=z, patience=patience, drift_z=drift_z)
             t0 = time.perf_counter()
             api.batch_run([m for m, _ in cold], workers=workers)
             ts_cold += time.perf_counter() - t0
@@ -227,8 +236,8 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
             for r, (mc, _), (mw, _), ref_k in zip(rows[len(rows) - len(chunk):], cold, warm, refs):
                 r["cold_stop"] = mc.steps_run()
                 r["warm_stop"] = mw.steps_run()
-                r["cold_stop_ok"], r["cold_stop_mean_ok"] = stopped_within(mc, ref_k, window, batches, patience)
-                r["warm_stop_ok"], r["warm_stop_mean_ok"] = stopped_within(mw, ref_k, window, batches, patience)
+                r["cold_stop_ok"], r["cold_stop_mean_ok"] = stopped_within(mc, ref_k, window, batches, patience, z, drift_z)
+                r["warm_stop_ok"], r["warm_stop_mean_ok"] = stopped_within(mw, ref_k, window, batches, patience, z, drift_z)
                 mc.close()
                 mw.close()
 
@@ -250,8 +259,8 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
         "steady_in_both": int(both.sum()),
         "never_steady_cold": int(sum(r["cold"] < 0 for r in rows)),
         "never_steady_warm": int(sum(r["warm"] < 0 for r in rows)),
-        "detector": f"windows of {window} steps ({batches} batch means) within 3 SE of the run's anchor window for "
-                    f"{patience} windows",
+        "detector": f"windows of {window} steps ({batches} batch means) within {z:g} SE of the run's anchor window for "
+                    f"{patience} windows" + (f", no trend beyond {drift_z:g} SE over them" if drift_z > 0 else ""),
         "mean_detector_onset_cold": float(onsets("cold_detector").mean()),
         "mean_detector_onset_warm": float(onsets("warm_detector").mean()),
         "rms_start_error_K_cold": float(np.sqrt(np.mean([r["cold_start_error_K"] ** 2 for r in rows]))),

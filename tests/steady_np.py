@@ -5,8 +5,10 @@ Windows of W recorded steps per sensor over (energy count, flux x, flux y), flux
 of its batch means and its standard error their spread over sqrt(B) (sums about the previous
 window's mean); window c agrees with the anchor window j when |m_c - m_j| <= z sqrt(se_c^2 +
 se_j^2) for all three, and a window that disagrees becomes the anchor (window 0 is the first);
-a sensor's onset is j*W for the first anchor j followed by M agreeing windows; the model's
-onset is the largest over the sensors, -1 when any sensor has none."""
+a sensor's onset is j*W for the first anchor j followed by M agreeing windows; with a trend
+tolerance zd > 0 those M + 1 windows must also show no least-squares slope of any quantity's
+window means beyond zd of its standard error (else the latest window becomes the anchor); the
+model's onset is the largest over the sensors, -1 when any sensor has none."""
 import numpy as np
 
 
@@ -14,7 +16,8 @@ def fixed_point(flux: np.ndarray) -> np.ndarray:
     return np.rint(flux * 1048576.0)
 
 
-def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: int, z: float, patience: int) -> np.ndarray:
+def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: int, z: float, patience: int,
+                  drift_z: float = 0.0) -> np.ndarray:
     S, K = energy.shape
     nw = K // window
     L = window // batches
@@ -28,6 +31,8 @@ def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: in
         anchor_se = np.zeros(3)
         anchor_w = 0
         streak = 0
+        n_w = s_i = s_ii = 0.0
+        s_d, s_id, v0, v1, v2 = ([0.0] * 3 for _ in range(5))
         for w in range(nw):
             mean = np.zeros(3)
             se = np.zeros(3)
@@ -39,13 +44,39 @@ def sensor_onsets(energy: np.ndarray, flux: np.ndarray, window: int, batches: in
                 mean[q] = prev_mean[q] + d
                 se[q] = np.sqrt(var / batches)
             agree = w > 0 and bool(np.all(np.abs(mean - anchor_mean) <= z * np.sqrt(se * se + anchor_se * anchor_se)))
+            reset = not agree
             if agree:
                 streak += 1
+                i = float(streak)
+                n_w += 1.0
+                s_i += i
+                s_ii += i * i
+                for q in range(3):
+                    d = mean[q] - anchor_mean[q]
+                    v = se[q] * se[q]
+                    s_d[q] += d
+                    s_id[q] += i * d
+                    v0[q] += v
+                    v1[q] += i * v
+                    v2[q] += i * i * v
                 if streak >= patience:
-                    out[s] = anchor_w * window
-                    break
-            else:
+                    flat = True
+                    if drift_z > 0.0:
+                        ib = s_i / n_w
+                        sxx = s_ii - n_w * ib * ib
+                        for q in range(3):
+                            slope = (s_id[q] - ib * s_d[q]) / sxx
+                            var = max(0.0, v2[q] - 2.0 * ib * v1[q] + ib * ib * v0[q]) / (sxx * sxx)
+                            flat = flat and abs(slope) <= drift_z * np.sqrt(var)
+                    if flat:
+                        out[s] = anchor_w * window
+                        break
+                    reset = True
+            if reset:
                 anchor_mean, anchor_se, anchor_w, streak = mean, se, w, 0
+                n_w, s_i, s_ii = 1.0, 0.0, 0.0
+                s_d, s_id, v1, v2 = [0.0] * 3, [0.0] * 3, [0.0] * 3, [0.0] * 3
+                v0 = [se[q] * se[q] for q in range(3)]
             prev_mean = mean
     return out
 

@@ -52,11 +52,25 @@ def test_restatement_sees_a_slow_drift():
     assert model_onset(sensor_onsets(energy, flux, 50, 5, 3.0, 3)) == 0
 
 
+def test_restatement_trend_test_sees_a_slower_drift():
+    """A drift of 0.1 per step (5 per 50-step window, under one standard error of a window mean)
+    stays within 3 combined standard errors of the anchor over 3 windows in most seeds, which are
+    then called steady early; the trend test over the anchor and those windows rejects most of
+    those early calls, and keeps a flat series with the same noise steady from the start."""
+    slow = [model_onset(sensor_onsets(*drifting_series(seed, rate=0.1), 50, 5, 3.0, 3)) for seed in range(20)]
+    trend = [model_onset(sensor_onsets(*drifting_series(seed, rate=0.1), 50, 5, 3.0, 3, drift_z=2.0)) for seed in range(20)]
+    early = lambda onsets: sum(0 <= o < 400 for o in onsets)
+    assert early(slow) >= 10 and early(trend) <= early(slow) // 2, (slow, trend)
+    flat = [model_onset(sensor_onsets(*drifting_series(seed, rate=0.0), 50, 5, 3.0, 3, drift_z=2.0)) for seed in range(20)]
+    assert sum(0 <= o <= 100 for o in flat) >= 15, flat
+
+
 def test_arguments_are_checked(built):
     from psim_gb300 import api
     e = np.zeros((2, 100), dtype=np.int64)
     f = np.zeros((2, 100, 2))
-    for kw in ({"window": 1, "batches": 1}, {"window": 50, "batches": 3}, {"batches": 1}, {"z": 0.0}, {"patience": 0}):
+    for kw in ({"window": 1, "batches": 1}, {"window": 50, "batches": 3}, {"batches": 1}, {"z": 0.0}, {"patience": 0},
+               {"drift_z": -1.0}, {"drift_z": float("nan")}):
         with pytest.raises(api.PsimError) as exc:
             api.steady_state(e, f, **kw)
         assert exc.value.code == api.PSIM_ERR_INVALID
@@ -75,12 +89,23 @@ def test_gpu_matches_restatement_on_synthetic_series(gpu, seed, window, batches,
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("seed,rate", [(0, 0.3), (1, 0.16), (2, 0.0)])
-def test_gpu_matches_restatement_on_drifting_series(gpu, seed, rate):
+@pytest.mark.parametrize("seed,rate,patience,drift_z", [(0, 0.3, 3, 0.0), (1, 0.16, 3, 0.0), (2, 0.0, 3, 0.0), (3, 0.1, 5, 2.0),
+                                                        (4, 0.1, 5, 2.0), (5, 0.0, 5, 2.0), (6, 0.05, 8, 2.5), (7, 0.1, 3, 2.0)])
+def test_gpu_matches_restatement_on_drifting_series(gpu, seed, rate, patience, drift_z):
     from psim_gb300 import api
     energy, flux = drifting_series(seed, rate)
-    onset, per = api.steady_state(energy, flux, window=50, batches=5, z=3.0, patience=3)
-    want = sensor_onsets(energy, flux, 50, 5, 3.0, 3)
+    onset, per = api.steady_state(energy, flux, window=50, batches=5, z=3.0, patience=patience, drift_z=drift_z)
+    want = sensor_onsets(energy, flux, 50, 5, 3.0, patience, drift_z)
+    assert np.array_equal(per, want) and onset == model_onset(want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [1, 3])
+def test_gpu_matches_restatement_with_the_trend_test(gpu, seed):
+    from psim_gb300 import api
+    energy, flux = relaxing_series(seed)
+    onset, per = api.steady_state(energy, flux, window=50, batches=5, z=3.0, patience=4, drift_z=2.0)
+    want = sensor_onsets(energy, flux, 50, 5, 3.0, 4, 2.0)
     assert np.array_equal(per, want) and onset == model_onset(want)
 
 
