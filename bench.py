@@ -13,7 +13,8 @@ so the budget is num_phonons = 1e7 * steps / L with L the mean lifetime in steps
 by an untimed pilot run of the same model.
 
 Outside the timed region the line also carries:
-  batch       256 independent random rectangles run concurrently (autotuned workers and grid)
+  batch       256 independent random rectangles run together (autotuned: batched launches fed by a
+              device work queue, or models on worker threads)
   warm_start  time to steady state (3 SE, against an independent longer run) of held-out
               rectangles started from the GPU-trained surrogate's temperatures vs the plain
               cold start
@@ -46,7 +47,7 @@ PER_STEP = 1.0e7
 STEPS = 5000
 DT_PS = 2.0
 BYTES_PER_PHONON_STEP = 64  # one 32-byte state record read and one written
-BATCH_CHUNK = 64  # batched models alive at once
+BATCH_CHUNK = 256  # batched models alive at once (state buffers follow each model's population)
 
 
 def dist_env():
@@ -241,7 +242,8 @@ def summarize_extras(steady, fp64_check, batch, warm, others) -> dict:
         out["fp32_vs_fp64_T"] = {k: fp64_check[k] for k in ("mean_abs_diff_K", "max_abs_diff_K", "seed_to_seed_sd_K")}
     if batch is not None:
         out["batch"] = {"value": batch["value"], "models": batch.get("models"), "alive_at_once": batch.get("alive_at_once"),
-                        "one_at_a_time": (batch.get("one_at_a_time") or {}).get("value")}
+                        "first_64": {k: (batch.get("first_64") or {}).get(k) for k in ("value", "worker_threads_value",
+                                                                                        "device_queue_value")}}
     if warm is not None:
         keep = ("mean_onset_steps_cold", "mean_onset_steps_warm", "steps_ratio_cold_over_warm",
                 "wall_ratio_cold_over_warm_to_steady_stop", "test_rmse_K", "stopped_within_3se_cold",
@@ -445,9 +447,9 @@ def main():
         fp64_check.update(precision_error(np.array(s32), np.array(s64)))
 
     # the batched workload: independent random rectangles (uneven cells and populations) run
-    # concurrently, options from the autotuner, in chunks of BATCH_CHUNK models alive at once
-    # (each model keeps device buffers sized for its run's phonons); the first chunk also runs
-    # one model at a time for comparison
+    # together with the autotuner's options (batched launches fed by a device work queue, or
+    # models on worker threads), BATCH_CHUNK models alive at once; the first 64 models also run one
+    # at a time, and with the worker-thread batch, for comparison
     batch = None
     if rank == 0 and world == 1 and args.batch_models > 0:
         from psim_gb300 import modelgen as mg
@@ -466,28 +468,33 @@ def main():
             secs += s_c
             steps_b += n_c
             if single is None:
+                first = models[:64]
                 t0 = time.perf_counter()
                 steps_s = 0
                 kernel_s = 0.0
-                for i, m in zip(ids, models):
+                for i, m in zip(ids, first):
                     m.run(seed=i + 1, precision=precision)
                     c1 = m.counters()
                     steps_s += c1["phonon_steps"]
                     kernel_s += c1["kernel_ms"] / 1e3
                 secs_s = time.perf_counter() - t0
+                s_t, n_t = api.batch_run(first, workers=16, device_queue=False)
+                s_q, n_q = api.batch_run(first, workers=16, device_queue=True, per_thread=opt.per_thread)
                 # device_value: the same models' phonon-steps over their transport-kernel time
                 # alone, the rate the batch would reach if concurrency added nothing
-                single = {"models": len(models), "value": steps_s / secs_s, "seconds": secs_s,
-                          "device_value": steps_s / kernel_s, "batched_value": n_c / s_c}
+                single = {"models": len(first), "value": steps_s / secs_s, "seconds": secs_s,
+                          "device_value": steps_s / kernel_s, "worker_threads_value": n_t / s_t,
+                          "device_queue_value": n_q / s_q}
             for m in models:
                 m.close()
         batch = {"workload": f"{args.batch_models} random rectangles: length U(0.2, 5) um, width U(50, 500) nm, 4-200 cells, "
                              "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
-                             f"3000 steps of 5 ps, steady state; run {BATCH_CHUNK} at a time",
-                 "autotuned": {"workers": opt.workers, "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate,
-                               "pilot_models": 8},
+                             f"3000 steps of 5 ps, steady state; {min(BATCH_CHUNK, args.batch_models)} alive at once",
+                 "autotuned": {"device_queue": opt.device_queue, "per_thread": opt.per_thread, "workers": opt.workers,
+                               "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": 8},
                  "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
-                 "one_at_a_time": single}
+                 "models": args.batch_models, "alive_at_once": min(BATCH_CHUNK, args.batch_models),
+                 "first_64": single}
 
     # the learned warm start: a surrogate trained on GPU Monte Carlo steady fields (outside the
     # timed region), held-out rectangles run cold and warm, each timed to steady state at 3 SE

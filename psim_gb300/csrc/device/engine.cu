@@ -22,6 +22,7 @@ namespace psim::gpu {
 
 void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem, cudaStream_t stream);
 void launch_batch_f32(const BatchLaunch& B, int grid, std::size_t smem, cudaStream_t stream);
+void launch_gather_counts(const std::uint32_t* const* ptrs, std::uint32_t n, std::uint32_t* out, cudaStream_t stream);
 int occupancy_batch_f32(std::size_t smem);
 std::size_t batch_static_smem();
 void launch_population_max(const std::uint32_t* population, std::uint32_t n, unsigned long long* counters, cudaStream_t stream);
@@ -1037,92 +1038,123 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
     if (occ <= 0) { return false; }
     const int grid = engines.front()->impl_->sms * occ;
 
-    // state buffers for every phonon of each run, cleared counters
-    for (Engine* E : engines) {
-        Impl& I = *E->impl_;
+    // state buffers that grow with each run's population (as a chunked single run's), cleared counters
+    const std::size_t M = engines.size();
+    std::vector<std::vector<std::uint64_t>> born(M);// newborns of steps [0, s) per model
+    for (std::size_t m = 0; m < M; ++m) {
+        Engine& E = *engines[m];
+        Impl& I = *E.impl_;
         if (I.state[0].bytes != I.capacity * 32) {
             I.state[0].release();
             I.state[1].release();
             I.capacity = 0;
         }
-        E->ensure_capacity(std::max<std::uint64_t>(I.total + 1024, 4096), 0, 0, 0, 32, false, stream);
+        born[m].assign(steps + 1, 0);
+        for (std::uint64_t k = 0; k < steps; ++k) { born[m][k + 1] = born[m][k] + I.n_new[k]; }
         check(cudaMemsetAsync(I.counts.p, 0, I.counts.bytes, stream), "memset counts");
         check(cudaMemsetAsync(I.counters.p, 0, I.counters.bytes, stream), "memset counters");
         check(cudaMemsetAsync(I.population.p, 0, I.population.bytes, stream), "memset population");
     }
-    // each launch's parameters of every model: params[w][m]
-    const std::size_t M = engines.size();
     std::vector<std::uint64_t> starts;
     for (std::uint64_t s0 = 0; s0 < steps; s0 += fused) { starts.push_back(s0); }
-    std::vector<StepParams> params(starts.size() * M);
+    // each model's launch parameters that stay the same (tables, layout of its staged tables)
+    std::vector<StepParams> base(M);
     for (std::size_t m = 0; m < M; ++m) {
-        const Engine& E = *engines[m];
         const Layout& L = lay[m];
-        StepParams base{};
-        E.base_params(base);
-        base.coast_lanes = 0U;
-        base.stage_mask = 7U;
-        base.off_cells = 0U;
-        base.off_alias = static_cast<std::uint32_t>(L.cells);
-        base.off_vel = static_cast<std::uint32_t>(L.cells + L.alias);
-        base.off_centre = static_cast<std::uint32_t>(L.cells + L.alias + L.vel);
-        base.off_sensors = static_cast<std::uint32_t>(L.cells + L.alias + L.vel + L.centre);
-        base.off_materials = static_cast<std::uint32_t>(base.off_sensors + L.sens);
-        base.off_emitters = static_cast<std::uint32_t>(base.off_materials + L.mat);
-        base.off_tally = static_cast<std::uint32_t>(L.tables());
-        for (std::size_t w = 0; w < starts.size(); ++w) {
-            StepParams P = base;
-            const std::uint64_t s0 = starts[w];
-            const auto tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, steps - s0));
-            if (E.window_steps(s0, tw, E.impl_->capacity) != tw) { return false; }// numbering beyond 32 bits
-            E.window_params(P, w, s0, tw);
-            params[w * M + m] = P;
-        }
+        StepParams& P = base[m];
+        engines[m]->base_params(P);
+        P.coast_lanes = 0U;
+        P.sort_mode = 0U;
+        P.stage_mask = 7U;
+        P.off_cells = 0U;
+        P.off_alias = static_cast<std::uint32_t>(L.cells);
+        P.off_vel = static_cast<std::uint32_t>(L.cells + L.alias);
+        P.off_centre = static_cast<std::uint32_t>(L.cells + L.alias + L.vel);
+        P.off_sensors = static_cast<std::uint32_t>(L.cells + L.alias + L.vel + L.centre);
+        P.off_materials = static_cast<std::uint32_t>(P.off_sensors + L.sens);
+        P.off_emitters = static_cast<std::uint32_t>(P.off_materials + L.mat);
+        P.off_tally = static_cast<std::uint32_t>(L.tables());
     }
+    // Launches in chunks: before each chunk every model's buffers are grown, where needed, to hold
+    // its survivors entering the chunk plus the chunk's newborns (one gathered read of the counts).
+    constexpr std::size_t kChunk = kLaunchesPerChunk;
     Buf d_params;
     Buf d_items;
-    d_params.upload(params);
+    Buf d_live;// [M][2] survivors entering the next chunk: front and back groups
+    d_params.alloc(std::min(kChunk, starts.size()) * M * sizeof(StepParams));
     d_items.alloc((M + 2) * sizeof(std::uint32_t));
+    d_live.alloc(M * 2 * sizeof(std::uint32_t));
+    std::vector<const std::uint32_t*> count_ptrs(2 * M);
+    Buf d_count_ptrs;
+    std::vector<std::uint32_t> live(2 * M, 0U);
+    std::vector<StepParams> params(std::min(kChunk, starts.size()) * M);
     BatchLaunch B{};
     B.item_begin = d_items.as<std::uint32_t>();
     B.item_next = d_items.as<std::uint32_t>() + M + 1;
     B.n_models = static_cast<std::uint32_t>(M);
     B.chunk = std::max<std::uint32_t>(1U, per_thread) * 1024U;
-
     cudaEvent_t ev0 = nullptr;
     cudaEvent_t ev1 = nullptr;
     check(cudaEventCreate(&ev0), "event");
     check(cudaEventCreate(&ev1), "event");
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
     float ms = 0.f;
+    std::uint64_t launches = 0;
     try {
-        check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-        for (std::size_t w = 0; w < starts.size(); ++w) {
-            B.params = d_params.as<StepParams>() + w * M;
-            launch_batch_f32(B, grid, smem, stream);
+        check(cudaEventRecord(ev0, stream), "event record");
+        for (std::size_t c0 = 0; c0 < starts.size(); c0 += kChunk) {
+            const std::size_t c1 = std::min(starts.size(), c0 + kChunk);
+            const std::uint64_t s_from = starts[c0];
+            const std::uint64_t s_to = c1 < starts.size() ? starts[c1] : steps;
+            if (c0 > 0) {
+                for (std::size_t m = 0; m < M; ++m) {
+                    const auto* counts = engines[m]->impl_->counts.as<std::uint32_t>();
+                    count_ptrs[2 * m] = counts + (c0 % 3);
+                    count_ptrs[2 * m + 1] = counts + 8 + (c0 % 3);
+                }
+                d_count_ptrs.upload(count_ptrs);
+                launch_gather_counts(d_count_ptrs.as<const std::uint32_t*>(), static_cast<std::uint32_t>(2 * M), d_live.as<std::uint32_t>(),
+                                     stream);
+                check(cudaMemcpyAsync(live.data(), d_live.p, 2 * M * sizeof(std::uint32_t), cudaMemcpyDeviceToHost, stream), "count read");
+                check(cudaStreamSynchronize(stream), "count read");
+            }
+            for (std::size_t m = 0; m < M; ++m) {
+                Engine& E = *engines[m];
+                E.ensure_capacity(static_cast<std::uint64_t>(live[2 * m]) + live[2 * m + 1] + (born[m][s_to] - born[m][s_from]) + 1024,
+                                  live[2 * m], live[2 * m + 1], static_cast<int>(c0 % 2), 32, true, stream);
+                for (std::size_t w = c0; w < c1; ++w) {
+                    StepParams P = base[m];
+                    const auto tw = static_cast<std::uint32_t>(std::min<std::uint64_t>(fused, steps - starts[w]));
+                    if (E.window_steps(starts[w], tw, E.impl_->capacity) != tw) {
+                        throw std::length_error("too many phonons in one step for 32-bit work indices");
+                    }
+                    E.window_params(P, w, starts[w], tw);
+                    params[(w - c0) * M + m] = P;
+                }
+            }
+            check(cudaMemcpyAsync(d_params.p, params.data(), (c1 - c0) * M * sizeof(StepParams), cudaMemcpyHostToDevice, stream),
+                  "batch parameters");
+            for (std::size_t w = c0; w < c1; ++w) {
+                B.params = d_params.as<StepParams>() + (w - c0) * M;
+                launch_batch_f32(B, grid, smem, stream);
+                launches += 2;
+            }
+            check(cudaGetLastError(), "batched launch");
+            // the parameter buffer is rewritten for the next chunk: its launches must have read it
+            if (c1 < starts.size()) { check(cudaStreamSynchronize(stream), "batch chunk"); }
         }
         for (Engine* E : engines) {
             Impl& I = *E->impl_;
             launch_population_max(I.population.as<std::uint32_t>(), static_cast<std::uint32_t>(steps), I.counters.as<unsigned long long>(),
                                   stream);
         }
-        check(cudaStreamEndCapture(stream, &graph), "end capture");
-        check(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
-        check(cudaEventRecord(ev0, stream), "event record");
-        check(cudaGraphLaunch(exec, stream), "graph launch");
         check(cudaEventRecord(ev1, stream), "event record");
         check(cudaStreamSynchronize(stream), "batch sync");
         check(cudaEventElapsedTime(&ms, ev0, ev1), "event time");
     } catch (...) {
-        if (exec != nullptr) { cudaGraphExecDestroy(exec); }
-        if (graph != nullptr) { cudaGraphDestroy(graph); }
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);
         throw;
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     // each run's counters; the batch's device time split by phonon-steps
@@ -1136,7 +1168,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         const double share = all > 0 ? static_cast<double>(st[m]) / static_cast<double>(all) : 1. / static_cast<double>(M);
         engines[m]->steps_run_ = steps;
         engines[m]->last_stage_mask_ = 7U;
-        engines[m]->finish_run(ms * share, 2 * starts.size() + 1, starts.size(), fused);
+        engines[m]->finish_run(ms * share, launches + 1, starts.size(), fused);
     }
     return true;
 }

@@ -795,6 +795,15 @@ void launch_step_f32(const StepParams& P, int grid, int block, std::size_t smem,
     }
 }
 
+// out[i] = *ptrs[i]: the survivor counts of a batch's models, read in one copy.
+__global__ void gather_counts_kernel(const std::uint32_t* const* ptrs, std::uint32_t n, std::uint32_t* out) {
+    for (std::uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) { out[i] = *ptrs[i]; }
+}
+
+void launch_gather_counts(const std::uint32_t* const* ptrs, std::uint32_t n, std::uint32_t* out, cudaStream_t stream) {
+    if (n > 0) { gather_counts_kernel<<<(n + 255) / 256, 256, 0, stream>>>(ptrs, n, out); }
+}
+
 void launch_batch_f32(const BatchLaunch& B, int grid, std::size_t smem, cudaStream_t stream) {
     batch_plan_kernel<<<1, 1024, 0, stream>>>(B);
     batch_kernel_f32<kStageCells | kStageTables><<<grid, 1024, smem, stream>>>(B);
