@@ -157,6 +157,17 @@ def cpu_sample(path_dir: str, budget: int, threads: int, seed: int, steps: int =
     return r.phonon_steps, r.seconds
 
 
+def demo_model(name: str, num_phonons: int = 0) -> dict:
+    """One of the reference's demo models kept in the test fixtures (gzipped psim JSON), with its
+    phonon budget replaced when num_phonons is given."""
+    import gzip
+    with gzip.open(os.path.join(ROOT, "tests", "golden", "models", name + ".json.gz"), "rt") as f:
+        d = json.load(f)
+    if num_phonons:
+        d["settings"]["num_phonons"] = int(num_phonons)
+    return d
+
+
 def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
     """The other single-model workloads, untimed by the headline: per model the device rate
     (phonon-steps / transport-kernel time), the end-to-end rate of psim_model_run (host wall
@@ -186,10 +197,15 @@ def other_workloads(td: str, precision: int, threads: int, cpu: bool) -> dict:
                           "2000 steps", full(budget(full, 2e5, 2000)), None),
         ("plate_transient", "4 x 1 um plate, 64 x 16 cells, transient, 400 K pulse on a 200 nm strip of the left edge "
                             "for 20 ps, 2e7 phonons, dt 1 ps, 3000 steps", mg.plate(), mg.plate(num_phonons=100000)),
+        ("reference_kinked_demo", "the reference's own kinked demo model (6174 cells, 3108 sensors: tables staged, cell "
+                                  "records and tallies in global memory), steady state, 5000 steps, its 2e7 budget",
+         demo_model("kinked_demo_120_35_spec"), demo_model("kinked_demo_120_35_spec", 100000)),
     ]
     out = {}
     for key, text, model, sample in cases:
         prec = api.FP64 if key.endswith("_fp64") else precision
+        if key == "reference_kinked_demo":
+            prec = api.FP32
         path = mg.write(model, os.path.join(td, key + ".json"))
         m = api.Model(path)
         m.run(seed=1, precision=prec)  # warm-up: tables, graph

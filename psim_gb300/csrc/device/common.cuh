@@ -268,6 +268,9 @@ struct StepParams {
     // Plain step boundaries (no edge impact and no scattering before the boundary) are crossed in
     // a warp-uniform loop while at least this many lanes of the warp can cross one (0: never)
     std::uint32_t coast_lanes;
+    // A warp takes new work items once at least this many of its lanes are free (1: as soon as
+    // one is), so that the start of new phonons runs on more lanes at once
+    std::uint32_t fetch_lanes;
     std::uint32_t new_begin[kMaxFused + 1];
     std::uint32_t id_base_f[kMaxFused];
     std::uint32_t group_begin_f[kMaxFused + 1];

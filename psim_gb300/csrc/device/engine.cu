@@ -822,6 +822,10 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     std::uint32_t fused = 1;
     P.coast_lanes = coast_lanes_;
+    P.fetch_lanes = 1U;
+    if (const char* fl = std::getenv("PSIM_GB300_FETCH"); fl != nullptr && std::atoi(fl) > 0) {
+        P.fetch_lanes = static_cast<std::uint32_t>(std::min(32, std::atoi(fl)));
+    }
     P.sort_mode = 0U;
     if (const char* so = std::getenv("PSIM_GB300_SORT"); so != nullptr && !fp64) {// "mode:value", value in steps or m/s
         const int mode = std::atoi(so);
@@ -1064,6 +1068,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         StepParams& P = base[m];
         engines[m]->base_params(P);
         P.coast_lanes = 0U;
+        P.fetch_lanes = 1U;
         P.sort_mode = 0U;
         P.stage_mask = 7U;
         P.off_cells = 0U;

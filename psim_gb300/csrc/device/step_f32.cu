@@ -502,7 +502,7 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
     while (true) {
         if (!exhausted) {
             const unsigned need = __ballot_sync(full, !active);
-            if (need != 0U) {
+            if (need != 0U && (static_cast<std::uint32_t>(__popc(need)) >= P.fetch_lanes || need == full)) {
                 const int leader = __ffs(static_cast<int>(need)) - 1;
                 std::uint32_t base = 0;
                 if (static_cast<int>(threadIdx.x & 31U) == leader) { base = fetch(static_cast<std::uint32_t>(__popc(need))); }
