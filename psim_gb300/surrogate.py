@@ -299,6 +299,9 @@ def main(argv=None) -> int:
     ap.add_argument("--eval-steps", type=int, default=6000, help="steps of the warm/cold evaluation runs")
     ap.add_argument("--scale", type=float, default=1.0, help="population scale of the generated models")
     ap.add_argument("--max-eval-length", type=float, default=2000.0, help="longest held-out rectangle (nm)")
+    ap.add_argument("--stop-z", type=float, default=STOP_Z, help="steady stop: agreement with the anchor window (SE)")
+    ap.add_argument("--stop-patience", type=int, default=STOP_PATIENCE, help="steady stop: agreeing windows")
+    ap.add_argument("--stop-drift", type=float, default=STOP_DRIFT_Z, help="steady stop: trend tolerance (SE, 0: none)")
     ap.add_argument("--out", default="")
     args = ap.parse_args(argv)
     t0 = time.perf_counter()
@@ -313,7 +316,8 @@ def main(argv=None) -> int:
     report = {"train_models": args.train, "epochs": args.epochs, "final_train_loss": loss,
               "test_mse_scaled": test_mse, "test_rmse_K": float(np.sqrt(test_mse) * T_SCALE),
               "generate_s": t_gen, "train_s": t_train}
-    report["warm_start"] = evaluate(net, held, steps=args.eval_steps, scale=args.scale)
+    report["warm_start"] = evaluate(net, held, steps=args.eval_steps, scale=args.scale, z=args.stop_z,
+                                    patience=args.stop_patience, drift_z=args.stop_drift)
     report["warm_start"]["held_out"] = f"rectangles of the training distribution up to {args.max_eval_length:g} nm long"
     text = json.dumps(report, indent=1)
     if args.out:

@@ -76,3 +76,27 @@ def test_precision_error_covers_temperature_and_flux():
     assert e["flux_y"]["max_abs_diff"] == 0.0 and e["flux_y"]["mean_diff_over_sd"] == 0.0
     sd = s64[:, :, 2].std(axis=0, ddof=1).mean()
     assert np.isclose(e["flux_x"]["mean_diff_over_sd"], (8.0 / 40) / sd)
+
+
+def test_extras_summary_is_short_and_keeps_each_measurement():
+    """The headline line carries the extra measurements' figures in a compact form (their full
+    records go on lines of their own before it), so the line stays short enough to be kept whole."""
+    steady = {"onset_step": -1, "onset_ns": None, "criterion": "x"}
+    fp = {"mean_abs_diff_K": 0.02, "max_abs_diff_K": 0.1, "seed_to_seed_sd_K": 0.04, "T": {}, "flux_x": {}}
+    batch = {"value": 1.2e10, "models": 256, "alive_at_once": 256,
+             "first_64": {"value": 7e9, "worker_threads_value": 9e9, "device_queue_value": 1.1e10, "seconds": 3.0}}
+    warm = {"mean_onset_steps_cold": 2400.0, "mean_onset_steps_warm": 600.0, "steps_ratio_cold_over_warm": 4.0,
+            "test_rmse_K": 0.2, "per_model": [1] * 500}
+    others = {"bar": {"value": 1e10, "e2e": 5e9, "precision": "fp64", "cpu_oracle": {"value": 1e8}, "workload": "w" * 300}}
+    ex = bench.summarize_extras(steady, fp, batch, warm, others)
+    assert ex["steady_onset_step"] == -1 and ex["batch"]["value"] == 1.2e10
+    assert ex["batch"]["first_64"]["device_queue_value"] == 1.1e10
+    assert ex["warm_start"]["steps_ratio_cold_over_warm"] == 4.0 and "per_model" not in ex["warm_start"]
+    assert ex["other_workloads"]["bar"] == {"value": 1e10, "e2e": 5e9, "precision": "fp64", "cpu": 1e8}
+    assert len(json.dumps(ex)) < 1200
+    assert bench.summarize_extras(None, None, None, None, None) == {}
+
+
+def test_demo_model_budget():
+    d = bench.demo_model("kinked_demo_120_35_spec", 12345)
+    assert d["settings"]["num_phonons"] == 12345 and len(d["cells"]) == 6174
