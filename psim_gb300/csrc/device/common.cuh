@@ -25,7 +25,7 @@ constexpr int kBins = 1000;
 constexpr int kAliasCols = 2048;             // 2 * kBins outcomes (bin, polarization) padded to 2^11
 constexpr std::uint32_t kNoEdge = 3U;
 constexpr int kMaxCollisions = 100;          // ModelSimulator MAX_COLLISIONS (psim/src/modelSimulator.cpp:25)
-constexpr unsigned kMaxEventsPerStep = 1U << 20; // hard bound on one phonon's events in one step
+constexpr unsigned kMaxEventsPerStep = 1U << 16; // hard bound on one phonon's events in one step
 constexpr float kFluxScale = 1048576.0f;     // flux tallies are fixed point: 2^20 units per m/s
 constexpr double kFluxScaleInv = 1.0 / 1048576.0;
 
@@ -326,8 +326,13 @@ struct BatchLaunch {
     const StepParams* params;
     std::uint32_t* item_begin;   // [n_models + 1], written by the plan kernel
     std::uint32_t* item_next;    // items handed out, cleared by the plan kernel
+    // [0] abort (1: a table staging timed out, 2: a model's event-limit hits ran past
+    // kBatchEventLimitAbort), [1] staging timeouts, [2] work items run, [3] stagings; once set, the
+    // abort ends every later item and launch at once and the host reports it
+    std::uint32_t* status;
     std::uint32_t n_models;
     std::uint32_t chunk;
 };
+constexpr unsigned long long kBatchEventLimitAbort = 4096;
 
 }// namespace psim::gpu

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <random>
@@ -1088,6 +1089,26 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
     Buf d_live;// [M][2] survivors entering the next chunk: front and back groups
     d_params.alloc(std::min(kChunk, starts.size()) * M * sizeof(StepParams));
     d_items.alloc((M + 2) * sizeof(std::uint32_t));
+    Buf d_status;
+    d_status.alloc(8 * sizeof(std::uint32_t));
+    check(cudaMemsetAsync(d_status.p, 0, d_status.bytes, stream), "memset status");
+    std::uint32_t status[8] = {};
+    const bool debug = std::getenv("PSIM_GB300_BATCH_DEBUG") != nullptr;
+    // The batch's status: fail with what the kernels recorded when they gave up.
+    auto check_status = [&](const char* where) {
+        check(cudaMemcpyAsync(status, d_status.p, sizeof status, cudaMemcpyDeviceToHost, stream), "batch status");
+        check(cudaStreamSynchronize(stream), "batch status");
+        if (debug) {
+            std::fprintf(stderr, "batch %s: abort %u, staging timeouts %u, items %u, stagings %u\n", where, status[0], status[1], status[2],
+                         status[3]);
+        }
+        if (status[0] != 0U) {
+            throw std::runtime_error(std::string("batched launches stopped (") + where + "): "
+                                     + (status[0] == 1U ? "a CUDA staging of model tables into shared memory timed out"
+                                                        : "a model's event-limit hits ran past the batch bound")
+                                     + ", " + std::to_string(status[2]) + " work items run, " + std::to_string(status[3]) + " stagings");
+        }
+    };
     d_live.alloc(M * 2 * sizeof(std::uint32_t));
     std::vector<const std::uint32_t*> count_ptrs(2 * M);
     Buf d_count_ptrs;
@@ -1096,6 +1117,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
     BatchLaunch B{};
     B.item_begin = d_items.as<std::uint32_t>();
     B.item_next = d_items.as<std::uint32_t>() + M + 1;
+    B.status = d_status.as<std::uint32_t>();
     B.n_models = static_cast<std::uint32_t>(M);
     B.chunk = std::max<std::uint32_t>(1U, per_thread) * 1024U;
     cudaEvent_t ev0 = nullptr;
@@ -1121,6 +1143,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
                                      stream);
                 check(cudaMemcpyAsync(live.data(), d_live.p, 2 * M * sizeof(std::uint32_t), cudaMemcpyDeviceToHost, stream), "count read");
                 check(cudaStreamSynchronize(stream), "count read");
+                check_status("between chunks");
             }
             for (std::size_t m = 0; m < M; ++m) {
                 Engine& E = *engines[m];
@@ -1155,6 +1178,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         check(cudaEventRecord(ev1, stream), "event record");
         check(cudaStreamSynchronize(stream), "batch sync");
         check(cudaEventElapsedTime(&ms, ev0, ev1), "event time");
+        check_status("at the end");
     } catch (...) {
         cudaEventDestroy(ev0);
         cudaEventDestroy(ev1);

@@ -649,12 +649,16 @@ __global__ void batch_plan_kernel(const __grid_constant__ BatchLaunch B) {
         for (std::uint32_t j = 0; j < P.n_fused; ++j) { atomicAdd(P.population + P.step + j, P.new_begin[j + 1U] - P.new_begin[j]); }
     }
     if (threadIdx.x == 0) {
+        const bool abort = *B.status != 0U;// a failed launch: the rest of the run has no work
         std::uint32_t acc = 0;
-        for (std::uint32_t m = 0; m < B.n_models; ++m) {
+        for (std::uint32_t m = 0; m < B.n_models && !abort; ++m) {
             const StepParams& P = B.params[m];
             B.item_begin[m] = acc;
             const std::uint32_t n = alive_in(P) + P.new_begin[P.n_fused];
             acc += (n + B.chunk - 1U) / B.chunk;
+        }
+        if (abort) {
+            for (std::uint32_t m = 0; m <= B.n_models; ++m) { B.item_begin[m] = 0U; }
         }
         B.item_begin[B.n_models] = acc;
         *B.item_next = 0U;
@@ -680,7 +684,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
     std::uint32_t steps = 0;
     while (true) {
         if (threadIdx.x == 0) {
-            const std::uint32_t it = atomicAdd(B.item_next, 1U);
+            const std::uint32_t it = *reinterpret_cast<volatile std::uint32_t*>(B.status) != 0U ? n_items : atomicAdd(B.item_next, 1U);
             std::uint32_t m = kNone;
             std::uint32_t lo = 0;
             std::uint32_t hi = 0;
@@ -728,15 +732,24 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
             tally_init(sP, bt, g_smem, sP.n_fused);
             const bool ok = mbar_wait_bounded(&stage_bar, parity);
             parity ^= 1U;
-            if (__syncthreads_or(!ok)) {// the copy did not complete: stop this block (reported)
-                if (threadIdx.x == 0) { atomicAdd(sP.counters + 5, 1ULL); }
+            if (__syncthreads_or(!ok)) {// the copy did not complete: stop this block and the batch (reported)
+                if (threadIdx.x == 0) {
+                    atomicAdd(sP.counters + 5, 1ULL);
+                    atomicAdd(B.status + 1, 1U);
+                    atomicExch(B.status, 1U);
+                }
                 mbar_wait_bounded(&stage_bar, parity ^ 1U);
                 return;
             }
+            if (threadIdx.x == 0) { atomicAdd(B.status + 3, 1U); }
             staged = m;
         }
         steps += lanes_run<S, false>(sP, s_alive, s_hi, [&](std::uint32_t k) { return s_lo + atomicAdd(&s_next, k); });
         __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicAdd(B.status + 2, 1U);
+            if (*reinterpret_cast<volatile unsigned long long*>(sP.counters + 4) > kBatchEventLimitAbort) { atomicExch(B.status, 2U); }
+        }
     }
 }
 

@@ -98,11 +98,19 @@ __device__ __forceinline__ bool mbar_try_wait(std::uint64_t* bar, unsigned parit
     return ok != 0U;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Bounded wait for the phase of the staging barrier with the given parity (0 for its first use);
-// false after the iteration limit.
+// false after the iteration limit or 200 ms, whichever comes first.
 __device__ __forceinline__ bool mbar_wait_bounded(std::uint64_t* bar, unsigned parity = 0U) {
+    const unsigned long long t0 = global_ns();
     for (unsigned it = 0; it < (1U << 22); ++it) {
         if (mbar_try_wait(bar, parity)) { return true; }
+        if ((it & 63U) == 63U && global_ns() - t0 > 200000000ULL) { return false; }
     }
     return false;
 }
