@@ -715,14 +715,16 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
         }
         __syncthreads();
         const std::uint32_t m = s_model;
-        if (m != staged) {
+        if (m != staged) {// a new model, or no more items (m == kNone): flush the model held
             if (staged != kNone) {// the previous model's tally and phonon-steps
                 block_count_add(sP.counters + 0, static_cast<unsigned long long>(steps));
                 steps = 0;
                 window_flush(sP, g_smem);
                 __syncthreads();
             }
-            if (m == kNone) { break; }
+        }
+        if (m == kNone) { break; }// also for a block that never took an item
+        if (m != staged) {
             const auto* src = reinterpret_cast<const std::uint32_t*>(B.params + m);
             auto* dst = reinterpret_cast<std::uint32_t*>(&sP);
             for (std::uint32_t i = threadIdx.x; i < sizeof(StepParams) / 4U; i += blockDim.x) { dst[i] = src[i]; }
