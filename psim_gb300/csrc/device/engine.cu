@@ -799,7 +799,9 @@ void Engine::run(int precision, void* stream_ptr) {
     // would not fit, so the buffers follow the peak population and no phonon is ever dropped.
     const std::uint64_t whole = std::max<std::uint64_t>(I.total + 1024, 4096);
     bool chunked = stop_on_ || whole * 2 * rec_bytes > kWholeRunStateBytes;
-    if (const char* ch = std::getenv("PSIM_GB300_CHUNKED"); ch != nullptr && std::atoi(ch) != 0) { chunked = true; }// test switch
+    if (const char* ch = std::getenv("PSIM_GB300_CHUNKED"); ch != nullptr) {// test and measurement switch
+        chunked = std::atoi(ch) != 0 || stop_on_;
+    }
     if (I.state[0].bytes != I.capacity * rec_bytes) {// first run, or the other precision's records
         I.state[0].release();
         I.state[1].release();

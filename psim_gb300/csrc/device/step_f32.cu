@@ -246,10 +246,11 @@ __device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, st
     L.events = 0;
 }
 
-template<unsigned S> __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive) {
+template<unsigned S>
+__device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::uint32_t i, std::uint32_t n_alive, std::uint32_t n_front) {
     if (i < n_alive) {
         const float4* in_pd = static_cast<const float4*>(P.in);
-        const std::uint32_t slot = slot_of(P, i);
+        const std::uint32_t slot = i < n_front ? i : P.capacity - 1U - (i - n_front);// front group, then the back group
         const float4 a = in_pd[slot];
         const uint4 b = reinterpret_cast<const uint4*>(in_pd + P.capacity)[slot];
         L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
@@ -492,7 +493,8 @@ template<unsigned S> __device__ __forceinline__ bool segment32(const StepParams&
 // the next item, so the warp stays full until the items run out instead of waiting for its
 // slowest phonon.  Returns the phonon-steps of this thread.
 template<unsigned S, bool kCoast, typename Fetch>
-__device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uint32_t n_alive, std::uint32_t total, Fetch fetch) {
+__device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uint32_t n_alive, std::uint32_t n_front, std::uint32_t total,
+                                                   Fetch fetch) {
     const unsigned full = 0xFFFFFFFFU;
     std::uint32_t steps = 0;// phonon-steps of this thread (a launch gives each thread far fewer than 2^32)
     bool active = false;
@@ -511,7 +513,7 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
                 if (!active) {
                     const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & ((1U << (threadIdx.x & 31U)) - 1U)));
                     if (i < total) {
-                        lane_start<S>(P, L, i, n_alive);
+                        lane_start<S>(P, L, i, n_alive, n_front);
                         active = true;
                     }
                 }
@@ -629,7 +631,8 @@ template<unsigned S, bool kCoast> __global__ void __launch_bounds__(1024, 1) ste
         }
     }
     const std::uint32_t total = n_alive + P.new_begin[P.n_fused];
-    const std::uint32_t steps = lanes_run<S, kCoast>(P, n_alive, total, [&](std::uint32_t k) { return atomicAdd(P.work, k); });
+    const std::uint32_t steps =
+        lanes_run<S, kCoast>(P, n_alive, min(*P.count_in, n_alive), total, [&](std::uint32_t k) { return atomicAdd(P.work, k); });
     block_count_add(P.counters + 0, static_cast<unsigned long long>(steps));
     window_flush(P, g_smem);
 }
@@ -674,7 +677,7 @@ __global__ void batch_plan_kernel(const __grid_constant__ BatchLaunch B) {
 template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32(const __grid_constant__ BatchLaunch B) {
     __shared__ std::uint64_t stage_bar;
     __shared__ __align__(16) StepParams sP;
-    __shared__ std::uint32_t s_model, s_lo, s_hi, s_alive, s_next;
+    __shared__ std::uint32_t s_model, s_lo, s_hi, s_alive, s_front, s_next;
     if (threadIdx.x == 0) { mbar_init(&stage_bar, 1U); }
     __syncthreads();
     const std::uint32_t n_items = B.item_begin[B.n_models];
@@ -689,6 +692,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
             std::uint32_t lo = 0;
             std::uint32_t hi = 0;
             std::uint32_t alive = 0;
+            std::uint32_t front = 0;
             if (it < n_items) {// the model owning item 'it': the last m with item_begin[m] <= it
                 std::uint32_t a = 0;
                 std::uint32_t b = B.n_models;
@@ -703,6 +707,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
                 m = a;
                 const StepParams& P = B.params[m];
                 alive = alive_in(P);
+                front = min(*P.count_in, alive);
                 const std::uint32_t total = alive + P.new_begin[P.n_fused];
                 lo = (it - B.item_begin[m]) * B.chunk;
                 hi = min(lo + B.chunk, total);
@@ -711,6 +716,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
             s_lo = lo;
             s_hi = hi;
             s_alive = alive;
+            s_front = front;
             s_next = 0U;
         }
         __syncthreads();
@@ -746,7 +752,7 @@ template<unsigned S> __global__ void __launch_bounds__(1024, 1) batch_kernel_f32
             if (threadIdx.x == 0) { atomicAdd(B.status + 3, 1U); }
             staged = m;
         }
-        steps += lanes_run<S, false>(sP, s_alive, s_hi, [&](std::uint32_t k) { return s_lo + atomicAdd(&s_next, k); });
+        steps += lanes_run<S, false>(sP, s_alive, s_front, s_hi, [&](std::uint32_t k) { return s_lo + atomicAdd(&s_next, k); });
         __syncthreads();
         if (threadIdx.x == 0) {
             atomicAdd(B.status + 2, 1U);

@@ -221,6 +221,20 @@ inline std::size_t tally_smem_bytes(std::uint32_t S, std::uint32_t slots = 1) {
 // with 'back', the back group (from the last slot down); returns the slot or UINT32_MAX.
 __device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool alive, bool back = false) {
     const unsigned full = 0xFFFFFFFFU;
+    if (P.sort_mode == 0U) {// one group: front only
+        const unsigned mask = __ballot_sync(full, alive);
+        const int lane = static_cast<int>(threadIdx.x & 31U);
+        std::uint32_t base = 0;
+        if (lane == 0 && mask != 0U) { base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(mask))); }
+        base = __shfl_sync(full, base, 0);
+        if (!alive) { return 0xFFFFFFFFU; }
+        const std::uint32_t slot = base + static_cast<std::uint32_t>(__popc(mask & ((1U << lane) - 1U)));
+        if (slot >= P.capacity) {
+            atomicAdd(P.counters + 2, 1ULL);
+            return 0xFFFFFFFFU;
+        }
+        return slot;
+    }
     const unsigned front_mask = __ballot_sync(full, alive && !back);
     const unsigned back_mask = __ballot_sync(full, alive && back);
     const int lane = static_cast<int>(threadIdx.x & 31U);
@@ -246,11 +260,6 @@ __device__ __forceinline__ std::uint32_t reserve_slot(const StepParams& P, bool 
 // Survivors entering a launch (both groups; beyond the buffer they were dropped and counted).
 __device__ __forceinline__ std::uint32_t alive_in(const StepParams& P) { return min(*P.count_in + *P.back_in, P.capacity); }
 
-// Buffer slot of survivor i: the front group first, then the back group from the last slot down.
-__device__ __forceinline__ std::uint32_t slot_of(const StepParams& P, std::uint32_t i) {
-    const std::uint32_t nf = *P.count_in;
-    return i < nf ? i : P.capacity - 1U - (i - nf);
-}
 
 __device__ __forceinline__ void block_count_add(unsigned long long* target, unsigned long long v) {
     const unsigned full = 0xFFFFFFFFU;

@@ -110,7 +110,10 @@ def test_rates_known_answers(api):
     reaches about 60 in germanium, where the Umklapp rate is the whole total.  Frequencies that
     round to the same float as the TA cut-off w are left out of the FP32 comparison: there the
     float comparison with w can take the other branch (Umklapp instead of normal scattering),
-    a choice the FP64 kernel makes exactly."""
+    a choice the FP64 kernel makes exactly.  Cases whose total rate is below 1 per second are left
+    out of the FP32 comparison too: germanium's TA Umklapp rate far above its branch maximum at
+    2 K is about 1e-36 per second, below the float range of e^-x, and a phonon with such a rate does
+    not scatter within any run (runs span nanoseconds)."""
     gold = np.load(os.path.join(GOLDEN, "rates.npz"))
     m = api.Model(model_path("si_ge_bar"))
     d = m.sim_desc()
@@ -133,9 +136,12 @@ def test_rates_known_answers(api):
         total = ref.sum(axis=1, keepdims=True)
         rel = np.abs(r32 - ref) / total
         at_cut = (np.float32(f / 1e13) == np.float32(params[i][4] / 1e13)) & (f != params[i][4])
-        print(f"{name} fp32: {int(at_cut.sum())} cases within float rounding of the cut-off left out")
-        rel = rel[~at_cut]
-        T, f = T[~at_cut], f[~at_cut]
+        negligible = total[:, 0] < 1.0
+        print(f"{name} fp32: {int(at_cut.sum())} cases within float rounding of the cut-off and "
+              f"{int((negligible & ~at_cut).sum())} with a total rate below 1/s left out")
+        keep = ~at_cut & ~negligible
+        rel = rel[keep]
+        T, f = T[keep], f[keep]
         print(f"{name} fp32: largest error {rel.max():.2e} of the total rate "
               f"(T {T[rel.max(axis=1).argmax()]:g} K, f {f[rel.max(axis=1).argmax()]:.4g} rad/s)")
         assert np.all(np.isfinite(r32))
