@@ -81,6 +81,11 @@ struct Buf {
 constexpr std::uint64_t kWholeRunStateBytes = std::uint64_t{ 512 } << 20;
 // Transport launches per chunk of a chunked run.
 constexpr std::uint64_t kLaunchesPerChunk = 16;
+// A warp of the FP32 kernel takes new work items once this many of its lanes are free: the start of
+// new phonons (a global work counter, state loads) then runs on several lanes at once.  Kinked
+// benchmark model, 2000 steps: 1 lane 1.818e10, 2: 1.852e10, 4: 1.886e10, 8: 1.860e10, 16: 1.739e10
+// phonon-steps/s (identical tallies).
+constexpr std::uint32_t kFetchLanes = 4;
 
 Line64 line64(psim::P2 a, psim::P2 b) {
     const psim::Seg64 s = psim::make_seg(a, b, nullptr);
@@ -825,7 +830,7 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     std::uint32_t fused = 1;
     P.coast_lanes = coast_lanes_;
-    P.fetch_lanes = 1U;
+    P.fetch_lanes = kFetchLanes;
     if (const char* fl = std::getenv("PSIM_GB300_FETCH"); fl != nullptr && std::atoi(fl) > 0) {
         P.fetch_lanes = static_cast<std::uint32_t>(std::min(32, std::atoi(fl)));
     }
@@ -1071,7 +1076,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         StepParams& P = base[m];
         engines[m]->base_params(P);
         P.coast_lanes = 0U;
-        P.fetch_lanes = 1U;
+        P.fetch_lanes = kFetchLanes;
         P.sort_mode = 0U;
         P.stage_mask = 7U;
         P.off_cells = 0U;
