@@ -478,7 +478,7 @@ def main():
             paths = [mg.write(mg.random_bar(1000 + i), os.path.join(td, f"rect_{i}.json")) for i in ids]
             models = [api.Model(p).set_options(seed=i + 1, precision=precision) for i, p in zip(ids, paths)]
             if opt is None:
-                opt, tuned_rate = api.batch_autotune(models, sample=min(8, len(models)))
+                opt, tuned_rate = api.batch_autotune(models, sample=min(16, len(models)))
             s_c, n_c = api.batch_run(models, workers=opt.workers, max_blocks=opt.max_blocks,
                                      device_queue=bool(opt.device_queue), per_thread=opt.per_thread)
             secs += s_c
@@ -507,7 +507,7 @@ def main():
                              "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
                              f"3000 steps of 5 ps, steady state; {min(BATCH_CHUNK, args.batch_models)} alive at once",
                  "autotuned": {"device_queue": opt.device_queue, "per_thread": opt.per_thread, "workers": opt.workers,
-                               "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": 8},
+                               "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": min(16, args.batch_models)},
                  "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
                  "models": args.batch_models, "alive_at_once": min(BATCH_CHUNK, args.batch_models),
                  "first_64": single}
