@@ -271,6 +271,9 @@ struct StepParams {
     // A warp takes new work items once at least this many of its lanes are free (1: as soon as
     // one is), so that the start of new phonons runs on more lanes at once
     std::uint32_t fetch_lanes;
+    // Work items a warp takes from the work counter at a time into a pool of its own (0: as many as
+    // it has free lanes)
+    std::uint32_t pool;
     std::uint32_t new_begin[kMaxFused + 1];
     std::uint32_t id_base_f[kMaxFused];
     std::uint32_t group_begin_f[kMaxFused + 1];

@@ -86,6 +86,9 @@ constexpr std::uint64_t kLaunchesPerChunk = 16;
 // benchmark model, 2000 steps: 1 lane 1.818e10, 2: 1.852e10, 4: 1.886e10, 8: 1.860e10, 16: 1.739e10
 // phonon-steps/s (identical tallies).
 constexpr std::uint32_t kFetchLanes = 4;
+// Work items a warp of the FP32 kernel takes from the work counter at a time (0: as many as it has
+// free lanes).
+constexpr std::uint32_t kWarpPool = 0;
 
 Line64 line64(psim::P2 a, psim::P2 b) {
     const psim::Seg64 s = psim::make_seg(a, b, nullptr);
@@ -830,6 +833,8 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     std::uint32_t fused = 1;
     P.coast_lanes = coast_lanes_;
+    P.pool = kWarpPool;
+    if (const char* pl = std::getenv("PSIM_GB300_POOL"); pl != nullptr) { P.pool = static_cast<std::uint32_t>(std::max(0, std::atoi(pl))); }
     P.fetch_lanes = kFetchLanes;
     if (const char* fl = std::getenv("PSIM_GB300_FETCH"); fl != nullptr && std::atoi(fl) > 0) {
         P.fetch_lanes = static_cast<std::uint32_t>(std::min(32, std::atoi(fl)));
@@ -1077,6 +1082,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         engines[m]->base_params(P);
         P.coast_lanes = 0U;
         P.fetch_lanes = kFetchLanes;
+        P.pool = kWarpPool;
         P.sort_mode = 0U;
         P.stage_mask = 7U;
         P.off_cells = 0U;

@@ -499,21 +499,53 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
     std::uint32_t steps = 0;// phonon-steps of this thread (a launch gives each thread far fewer than 2^32)
     bool active = false;
     bool exhausted = false;// warp-uniform: the step's work counter has run out
+    // With P.pool > 0 the warp takes runs of P.pool items from the counter into a pool of its own
+    // [pool_lo, pool_hi) (warp-uniform) and hands them to its free lanes from there; each new run's
+    // state records are prefetched into L2 when the run is taken, ahead of the lanes that start them.
+    std::uint32_t pool_lo = 0;
+    std::uint32_t pool_hi = 0;
+    bool drained = false;// warp-uniform: the counter has handed out its last run
     Lane L;
     L.p = Ph32{ 0.f, 0.f, 0.f, 0.f, 0U, 0U, 0.f, 0U };
     while (true) {
         if (!exhausted) {
             const unsigned need = __ballot_sync(full, !active);
             if (need != 0U && (static_cast<std::uint32_t>(__popc(need)) >= P.fetch_lanes || need == full)) {
+                const int lane = static_cast<int>(threadIdx.x & 31U);
                 const int leader = __ffs(static_cast<int>(need)) - 1;
+                const auto want = static_cast<std::uint32_t>(__popc(need));
                 std::uint32_t base = 0;
-                if (static_cast<int>(threadIdx.x & 31U) == leader) { base = fetch(static_cast<std::uint32_t>(__popc(need))); }
-                base = __shfl_sync(full, base, leader);
-                if (base + static_cast<std::uint32_t>(__popc(need)) >= total) { exhausted = true; }
+                std::uint32_t avail = 0;
+                if (P.pool == 0U) {
+                    if (lane == leader) { base = fetch(want); }
+                    base = __shfl_sync(full, base, leader);
+                    if (base + want >= total) { exhausted = true; }
+                    avail = base < total ? min(want, total - base) : 0U;
+                } else {
+                    if (pool_lo == pool_hi && !drained) {
+                        std::uint32_t run = 0;
+                        if (lane == leader) { run = fetch(P.pool); }
+                        run = __shfl_sync(full, run, leader);
+                        pool_lo = min(run, total);
+                        pool_hi = min(run + P.pool, total);
+                        drained = run + P.pool >= total;
+                        const std::uint32_t k = pool_lo + static_cast<std::uint32_t>(lane);
+                        if (k < pool_hi && k < n_alive) {// survivors' records: bring them into L2 now
+                            const std::uint32_t slot = k < n_front ? k : P.capacity - 1U - (k - n_front);
+                            const float4* in_pd = static_cast<const float4*>(P.in);
+                            asm volatile("prefetch.global.L2 [%0];" ::"l"(in_pd + slot));
+                            asm volatile("prefetch.global.L2 [%0];" ::"l"(in_pd + P.capacity + slot));
+                        }
+                    }
+                    base = pool_lo;
+                    avail = min(want, pool_hi - pool_lo);
+                    pool_lo += avail;
+                    if (drained && pool_lo == pool_hi) { exhausted = true; }
+                }
                 if (!active) {
-                    const std::uint32_t i = base + static_cast<std::uint32_t>(__popc(need & ((1U << (threadIdx.x & 31U)) - 1U)));
-                    if (i < total) {
-                        lane_start<S>(P, L, i, n_alive, n_front);
+                    const std::uint32_t rank = static_cast<std::uint32_t>(__popc(need & ((1U << lane) - 1U)));
+                    if (rank < avail) {
+                        lane_start<S>(P, L, base + rank, n_alive, n_front);
                         active = true;
                     }
                 }
