@@ -274,6 +274,9 @@ struct StepParams {
     // Work items a warp takes from the work counter at a time into a pool of its own (0: as many as
     // it has free lanes)
     std::uint32_t pool;
+    // 1: the loop tail issues the output counter's atomic before the tallies and the next step's
+    // set-up and reads it after them
+    std::uint32_t tail_order;
     std::uint32_t new_begin[kMaxFused + 1];
     std::uint32_t id_base_f[kMaxFused];
     std::uint32_t group_begin_f[kMaxFused + 1];

@@ -89,6 +89,8 @@ constexpr std::uint32_t kFetchLanes = 4;
 // Work items a warp of the FP32 kernel takes from the work counter at a time (0: as many as it has
 // free lanes).
 constexpr std::uint32_t kWarpPool = 0;
+// 1: the FP32 kernel's loop tail overlaps the output counter's atomic with the tallies.
+constexpr std::uint32_t kTailOrder = 0;
 
 Line64 line64(psim::P2 a, psim::P2 b) {
     const psim::Seg64 s = psim::make_seg(a, b, nullptr);
@@ -833,6 +835,8 @@ void Engine::run(int precision, void* stream_ptr) {
     }
     std::uint32_t fused = 1;
     P.coast_lanes = coast_lanes_;
+    P.tail_order = kTailOrder;
+    if (const char* to = std::getenv("PSIM_GB300_TAIL"); to != nullptr) { P.tail_order = std::atoi(to) != 0 ? 1U : 0U; }
     P.pool = kWarpPool;
     if (const char* pl = std::getenv("PSIM_GB300_POOL"); pl != nullptr) { P.pool = static_cast<std::uint32_t>(std::max(0, std::atoi(pl))); }
     P.fetch_lanes = kFetchLanes;
@@ -1083,6 +1087,7 @@ bool Engine::run_batched(const std::vector<Engine*>& engines, void* stream_ptr, 
         P.coast_lanes = 0U;
         P.fetch_lanes = kFetchLanes;
         P.pool = kWarpPool;
+        P.tail_order = kTailOrder;
         P.sort_mode = 0U;
         P.stage_mask = 7U;
         P.off_cells = 0U;

@@ -591,8 +591,32 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
         const bool crossing = finishing && o.alive;// into step L.step + 1
         const bool stays = crossing && o.cont;
         steps += (finishing && o.boundary) ? 1U : 0U;
+        const bool leaving = crossing && !stays;
+        if (P.tail_order != 0U && P.sort_mode == 0U) {
+            // the output counter's atomic first; the tallies and the next step's set-up, which do
+            // not need its result, run while it is in flight; then the slot and the store
+            const unsigned out_mask = __ballot_sync(full, leaving);
+            const int lane = static_cast<int>(threadIdx.x & 31U);
+            std::uint32_t out_base = 0;
+            if (lane == 0 && out_mask != 0U) { out_base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(out_mask))); }
+            window_add(P, g_smem, crossing, o.tallied, L.step() - P.step, o.sensor, meta_sign(L.p.meta), o.fx, o.fy);
+            if (stays) { lane_enter_step(P, L, L.step() + 1U); }
+            out_base = __shfl_sync(full, out_base, 0);
+            if (leaving) {
+                const std::uint32_t slot = out_base + static_cast<std::uint32_t>(__popc(out_mask & ((1U << lane) - 1U)));
+                if (slot < P.capacity) {
+                    float4* out_pd = static_cast<float4*>(P.out);
+                    out_pd[slot] = make_float4(L.p.px, L.p.py, L.p.dx, L.p.dy);
+                    reinterpret_cast<uint4*>(out_pd + P.capacity)[slot] = make_uint4(L.p.meta, L.p.binw, __float_as_uint(L.p.tts), L.p.id);
+                } else {
+                    atomicAdd(P.counters + 2, 1ULL);
+                }
+            }
+            if (finishing && !stays) { active = false; }
+            continue;
+        }
         const bool back = P.sort_mode == 1U ? L.p.tts < P.sort_after : (P.sort_mode == 2U && L.v >= P.sort_after);
-        const std::uint32_t slot = reserve_slot(P, crossing && !stays, back);
+        const std::uint32_t slot = reserve_slot(P, leaving, back);
         if (slot != 0xFFFFFFFFU) {// records: float4 {px, py, dx, dy}[capacity], then uint4 {meta, binw, tts, id}[capacity]
             float4* out_pd = static_cast<float4*>(P.out);
             out_pd[slot] = make_float4(L.p.px, L.p.py, L.p.dx, L.p.dy);
