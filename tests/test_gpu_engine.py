@@ -69,16 +69,21 @@ def test_steps_per_launch_do_not_change_results(api, monkeypatch, tmp_path, name
     path = (mg.write(mg.plate(nx=64, ny=40, num_phonons=30000, num_measurements=120, sim_time=0.12),
                      os.path.join(str(tmp_path), "plate_2560.json")) if name == "plate_2560" else model_path(name))
     ref = None
-    # (staging, steps per launch, coasting lanes, survivor grouping, chunked run with growing buffers)
-    for stage, fuse, coast, sort, chunked in (("1", "1", "0", "0", "0"), ("1", "3", "16", "0", "0"), ("1", "8", "1", "0", "0"),
-                                              ("1", "16", "32", "0", "0"), ("0", "5", "16", "0", "0"), ("2", "7", "16", "0", "0"),
-                                              ("2", "2", "0", "0", "0"), ("1", "8", "0", "1:9", "0"), ("1", "6", "0", "2:5000", "1"),
-                                              ("1", "4", "0", "1:4", "1")):
+    # (staging, steps per launch, coasting lanes, survivor grouping, chunked run with growing buffers,
+    # free lanes per fetch, warp work pool, overlapped loop tail)
+    for stage, fuse, coast, sort, chunked, fetch, pool, tail in (
+            ("1", "1", "0", "0", "0", "1", "0", "0"), ("1", "3", "16", "0", "0", "4", "0", "0"), ("1", "8", "1", "0", "0", "4", "0", "0"),
+            ("1", "16", "32", "0", "0", "2", "0", "0"), ("0", "5", "16", "0", "0", "4", "0", "0"), ("2", "7", "16", "0", "0", "4", "0", "0"),
+            ("2", "2", "0", "0", "0", "8", "0", "0"), ("1", "8", "0", "1:9", "0", "4", "0", "0"), ("1", "6", "0", "2:5000", "1", "4", "0", "0"),
+            ("1", "4", "0", "1:4", "1", "4", "0", "0"), ("1", "9", "0", "0", "1", "4", "32", "1"), ("0", "3", "0", "0", "0", "1", "64", "1")):
         monkeypatch.setenv("PSIM_GB300_STAGE", stage)
         monkeypatch.setenv("PSIM_GB300_FUSE", fuse)
         monkeypatch.setenv("PSIM_GB300_COAST", coast)
         monkeypatch.setenv("PSIM_GB300_SORT", sort)
         monkeypatch.setenv("PSIM_GB300_CHUNKED", chunked)
+        monkeypatch.setenv("PSIM_GB300_FETCH", fetch)
+        monkeypatch.setenv("PSIM_GB300_POOL", pool)
+        monkeypatch.setenv("PSIM_GB300_TAIL", tail)
         m = api.Model(path)
         m.run(seed=11)
         e, f = m.tallies()
@@ -97,6 +102,8 @@ def test_steps_per_launch_do_not_change_results(api, monkeypatch, tmp_path, name
     monkeypatch.delenv("PSIM_GB300_COAST")
     monkeypatch.delenv("PSIM_GB300_SORT")
     monkeypatch.delenv("PSIM_GB300_CHUNKED")
+    for var in ("PSIM_GB300_FETCH", "PSIM_GB300_POOL", "PSIM_GB300_TAIL"):
+        monkeypatch.delenv(var)
 
 
 def test_counters_and_phonon_steps(api):
