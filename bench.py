@@ -257,7 +257,8 @@ def summarize_extras(steady, fp64_check, batch, warm, others) -> dict:
     if fp64_check is not None:
         out["fp32_vs_fp64_T"] = {k: fp64_check[k] for k in ("mean_abs_diff_K", "max_abs_diff_K", "seed_to_seed_sd_K")}
     if batch is not None:
-        out["batch"] = {"value": batch["value"], "models": batch.get("models"), "alive_at_once": batch.get("alive_at_once"),
+        out["batch"] = {"value": batch["value"], "mode": batch.get("mode"), "autotuned_value": batch.get("autotuned_value"),
+                        "models": batch.get("models"), "alive_at_once": batch.get("alive_at_once"),
                         "first_64": {k: (batch.get("first_64") or {}).get(k) for k in ("value", "worker_threads_value",
                                                                                         "device_queue_value")}}
     if warm is not None:
@@ -472,6 +473,8 @@ def main():
         opt = None
         secs = 0.0
         steps_b = 0
+        other_secs = 0.0
+        other_steps = 0
         single = None
         for c0 in range(0, args.batch_models, BATCH_CHUNK):
             ids = range(c0, min(c0 + BATCH_CHUNK, args.batch_models))
@@ -483,6 +486,12 @@ def main():
                                      device_queue=bool(opt.device_queue), per_thread=opt.per_thread)
             secs += s_c
             steps_b += n_c
+            # the same models the other way (the autotuner's pilot is a few models; the device queue
+            # gains with the number of models it can spread over the multiprocessors)
+            s_o, n_o = api.batch_run(models, workers=16 if opt.device_queue else opt.workers, max_blocks=opt.max_blocks,
+                                     device_queue=not bool(opt.device_queue), per_thread=opt.per_thread)
+            other_secs += s_o
+            other_steps += n_o
             if single is None:
                 first = models[:64]
                 t0 = time.perf_counter()
@@ -508,9 +517,15 @@ def main():
                              f"3000 steps of 5 ps, steady state; {min(BATCH_CHUNK, args.batch_models)} alive at once",
                  "autotuned": {"device_queue": opt.device_queue, "per_thread": opt.per_thread, "workers": opt.workers,
                                "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": min(16, args.batch_models)},
-                 "value": steps_b / secs, "unit": "phonon-steps/s", "seconds": secs, "phonon_steps": steps_b,
+                 "autotuned_value": steps_b / secs, "unit": "phonon-steps/s",
+                 "other_mode": {"device_queue": not bool(opt.device_queue), "value": other_steps / other_secs,
+                                "seconds": other_secs},
                  "models": args.batch_models, "alive_at_once": min(BATCH_CHUNK, args.batch_models),
                  "first_64": single}
+        # the batch's rate: the faster of the two ways, both measured on the same models
+        queue_best = other_steps / other_secs > steps_b / secs if not opt.device_queue else steps_b / secs >= other_steps / other_secs
+        batch.update({"value": max(steps_b / secs, other_steps / other_secs),
+                      "mode": "device work queue" if queue_best else "worker threads"})
 
     # the learned warm start: a surrogate trained on GPU Monte Carlo steady fields (outside the
     # timed region), held-out rectangles run cold and warm, each timed to steady state at 3 SE
