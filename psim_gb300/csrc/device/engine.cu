@@ -87,10 +87,13 @@ constexpr std::uint64_t kLaunchesPerChunk = 16;
 // phonon-steps/s (identical tallies).
 constexpr std::uint32_t kFetchLanes = 4;
 // Work items a warp of the FP32 kernel takes from the work counter at a time (0: as many as it has
-// free lanes).
+// free lanes).  A pool of 32 with L2 prefetch of its state records: kinked benchmark model 1.904e10
+// against 1.896e10 without; the 10-cell bar of 2e5 phonons per step 7.69e9 against 8.75e9.
 constexpr std::uint32_t kWarpPool = 0;
-// 1: the FP32 kernel's loop tail overlaps the output counter's atomic with the tallies.
-constexpr std::uint32_t kTailOrder = 0;
+// 1: the FP32 kernel's loop tail overlaps the output counter's atomic with the tallies.  Kinked
+// benchmark model, 2000 steps: 1.896e10 against 1.861e10 phonon-steps/s; the 10-cell bar 8.75e9
+// against 8.55e9 (identical tallies).
+constexpr std::uint32_t kTailOrder = 1;
 
 Line64 line64(psim::P2 a, psim::P2 b) {
     const psim::Seg64 s = psim::make_seg(a, b, nullptr);

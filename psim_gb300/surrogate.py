@@ -69,10 +69,12 @@ def _models(seeds: Sequence[int], td: str, *, periodic: bool, steps: int, scale:
 CHUNK = 128  # models alive at once: each keeps GPU buffers sized for its run's phonons
 
 # The steady stop of the evaluation's runs: agreement with the anchor window at STOP_Z standard
-# errors for STOP_PATIENCE windows, and (STOP_DRIFT_Z > 0) no trend over them beyond STOP_DRIFT_Z.
+# errors for STOP_PATIENCE windows, and (STOP_DRIFT_Z > 0) no trend over them beyond STOP_DRIFT_Z;
+# checked every STOP_EVERY steps (0: every STOP_PATIENCE + 1 windows).
 STOP_Z = 3.0
 STOP_PATIENCE = 3
 STOP_DRIFT_Z = 0.0
+STOP_EVERY = 0
 
 
 def generate(seeds: Sequence[int], *, steps: int = 3000, scale: float = 1.0, workers: int = 16) -> Tuple[np.ndarray, np.ndarray]:
@@ -176,7 +178,7 @@ def stopped_within(m: api.Model, ref: Tuple[np.ndarray, np.ndarray, int], window
 
 def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: float = 1.0, window: int = 100,
              batches: int = 5, patience: int = STOP_PATIENCE, z: float = STOP_Z, drift_z: float = STOP_DRIFT_Z,
-             workers: int = 16) -> Dict:
+             every: int = STOP_EVERY, workers: int = 16) -> Dict:
     """Cold and warm starts of the rectangles drawn from ``seeds``.
 
     A third, twice as long, warm-started run of each rectangle with its own seed gives the steady
@@ -226,7 +228,7 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
                              "start_error_K": float(np.sqrt(np.mean((tw[:, 0] - t_inf) ** 2))),
                              "cold_start_error_K": float(np.sqrt(np.mean((tc[:, 0] - t_inf) ** 2)))})
             for m, _ in cold + warm:
-                m.set_steady_stop(window=window, batches=batches, z=z, patience=patience, drift_z=drift_z)
+                m.set_steady_stop(window=window, batches=batches, z=z, patience=patience, drift_z=drift_z, check_every=every)
             t0 = time.perf_counter()
             api.batch_run([m for m, _ in cold], workers=workers)
             ts_cold += time.perf_counter() - t0
@@ -260,7 +262,8 @@ def evaluate(net: api.Mlp, seeds: Sequence[int], *, steps: int = 3000, scale: fl
         "never_steady_cold": int(sum(r["cold"] < 0 for r in rows)),
         "never_steady_warm": int(sum(r["warm"] < 0 for r in rows)),
         "detector": f"windows of {window} steps ({batches} batch means) within {z:g} SE of the run's anchor window for "
-                    f"{patience} windows" + (f", no trend beyond {drift_z:g} SE over them" if drift_z > 0 else ""),
+                    f"{patience} windows" + (f", no trend beyond {drift_z:g} SE over them" if drift_z > 0 else "")
+                    + f"; the stop checked every {every if every > 0 else (patience + 1) * window} steps",
         "mean_detector_onset_cold": float(onsets("cold_detector").mean()),
         "mean_detector_onset_warm": float(onsets("warm_detector").mean()),
         "rms_start_error_K_cold": float(np.sqrt(np.mean([r["cold_start_error_K"] ** 2 for r in rows]))),
@@ -302,6 +305,7 @@ def main(argv=None) -> int:
     ap.add_argument("--stop-z", type=float, default=STOP_Z, help="steady stop: agreement with the anchor window (SE)")
     ap.add_argument("--stop-patience", type=int, default=STOP_PATIENCE, help="steady stop: agreeing windows")
     ap.add_argument("--stop-drift", type=float, default=STOP_DRIFT_Z, help="steady stop: trend tolerance (SE, 0: none)")
+    ap.add_argument("--stop-every", type=int, default=STOP_EVERY, help="steady stop: steps between checks (0: patience + 1 windows)")
     ap.add_argument("--out", default="")
     args = ap.parse_args(argv)
     t0 = time.perf_counter()
@@ -317,7 +321,7 @@ def main(argv=None) -> int:
               "test_mse_scaled": test_mse, "test_rmse_K": float(np.sqrt(test_mse) * T_SCALE),
               "generate_s": t_gen, "train_s": t_train}
     report["warm_start"] = evaluate(net, held, steps=args.eval_steps, scale=args.scale, z=args.stop_z,
-                                    patience=args.stop_patience, drift_z=args.stop_drift)
+                                    patience=args.stop_patience, drift_z=args.stop_drift, every=args.stop_every)
     report["warm_start"]["held_out"] = f"rectangles of the training distribution up to {args.max_eval_length:g} nm long"
     text = json.dumps(report, indent=1)
     if args.out:
