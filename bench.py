@@ -263,7 +263,8 @@ def summarize_extras(steady, fp64_check, batch, warm, others) -> dict:
                                                                                         "device_queue_value")}}
     if warm is not None:
         keep = ("mean_onset_steps_cold", "mean_onset_steps_warm", "steps_ratio_cold_over_warm",
-                "wall_ratio_cold_over_warm_to_steady_stop", "test_rmse_K", "stopped_within_3se_cold",
+                "wall_ratio_cold_over_warm_to_steady_stop", "mean_steps_run_cold_to_steady_stop",
+                "mean_steps_run_warm_to_steady_stop", "test_rmse_K", "stopped_within_3se_cold",
                 "stopped_within_3se_warm", "held_out_models", "train_fields")
         out["warm_start"] = {k: warm[k] for k in keep if k in warm}
     if others is not None:

@@ -234,7 +234,10 @@ struct Outcome {
 };
 
 // The lane's phonon enters 'step' at its start: that step's random stream, a full step of time.
-// The same state is what a later launch would read back from the output buffer.
+// The same state is what a later launch would read back from the output buffer.  The rates of
+// its last scattering-time draw stay valid (the scattering event uses the draw's rates,
+// modelSimulator.cpp:148-153 and 186-187, and a run's sensor parameters do not change between
+// steps); a phonon read back from the buffer recomputes them (lane_start).
 __device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, std::uint32_t step) {
     L.rs.init(P.key0, P.key1, step, L.p.id);
     L.rem = P.dt;
@@ -242,7 +245,6 @@ __device__ __forceinline__ void lane_enter_step(const StepParams& P, Lane& L, st
     // make them here, where most lanes of the warp start a step together.
     if (L.p.tts < L.rem) { L.rs.prefill(); }
     L.need_target = true;
-    L.rates_ok = false;
     L.events = 0;
 }
 
@@ -255,6 +257,7 @@ __device__ __forceinline__ void lane_start(const StepParams& P, Lane& L, std::ui
         const uint4 b = reinterpret_cast<const uint4*>(in_pd + P.capacity)[slot];
         L.p = Ph32{ a.x, a.y, a.z, a.w, b.x, b.y, __uint_as_float(b.z), b.w };
         lane_enter_step(P, L, P.step);
+        L.rates_ok = false;
     } else {
         const std::uint32_t k = i - n_alive;
         std::uint32_t jf = 0;
@@ -296,7 +299,6 @@ __device__ __forceinline__ void lane_enter_step_lazy(const StepParams& P, Lane& 
     L.rs.init(P.key0, P.key1, step, L.p.id);
     L.rem = P.dt;
     L.need_target = true;
-    L.rates_ok = false;
     L.events = 0;
 }
 
@@ -459,9 +461,14 @@ template<unsigned S> __device__ __forceinline__ bool segment32(const StepParams&
     L.rem -= used;
     p.tts -= used;
     L.need_target = true;
-    if (L.rem == 0.f) { return boundary_outcome(P, L, out); }
+    if (L.rem == 0.f) {
+        // a new sensor area reached exactly at the boundary: its scattering rates are recomputed
+        // at the next event, as they are after a launch boundary
+        if (L.changed) { L.rates_ok = false; }
+        return boundary_outcome(P, L, out);
+    }
     if (!P.phasor_sim && p.tts == 0.f) {// ModelSimulator::scatter (modelSimulator.cpp:124-137)
-        if (!L.rates_ok) {// the scattering time was drawn in an earlier step: recompute its rates
+        if (!L.rates_ok) {// the scattering time was drawn before this launch: recompute its rates
             const float3 r = rates32(materials_of<S>(P)[L.mat], sensors_of<S>(P)[L.sensor], omega32<S>(P, p.binw, phasor), meta_pol(p.meta));
             const float inv = __frcp_rn(r.x + r.y + r.z);
             L.fN = r.x * inv;

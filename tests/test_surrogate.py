@@ -67,17 +67,32 @@ class _StoppedRun:
 
 def test_stopped_run_accuracy():
     from psim_gb300 import surrogate as sg
+    RULE = sg.StopRule(50, 5, 3.0, 3)
     rng = np.random.default_rng(5)
     t_inf = np.array([300.0, 305.0, 310.0])
     ref = sg.steady_reference(t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 4000)), 50)
     steady = t_inf[:, None] + rng.normal(0.0, 0.5, size=(3, 600))
-    assert sg.stopped_within(_StoppedRun(steady, 200), ref, 50, 5, 3) == (True, True)
+    assert sg.stopped_within(_StoppedRun(steady, 200), ref, 50, RULE) == (True, True)
     # stopped while still a kelvin away: both standards miss
-    assert sg.stopped_within(_StoppedRun(steady - 1.0, 200), ref, 50, 5, 3) == (False, False)
+    assert sg.stopped_within(_StoppedRun(steady - 1.0, 200), ref, 50, RULE) == (False, False)
     # a tenth of a kelvin off: inside one window's bound, outside the bound of a 400-step mean
-    assert sg.stopped_within(_StoppedRun(steady - 0.1, 200), ref, 50, 5, 3) == (True, False)
+    assert sg.stopped_within(_StoppedRun(steady - 0.1, 200), ref, 50, RULE) == (True, False)
     # no onset: the last window is taken
-    assert sg.stopped_within(_StoppedRun(steady, -1), ref, 50, 5, 3) == (True, True)
+    assert sg.stopped_within(_StoppedRun(steady, -1), ref, 50, RULE) == (True, True)
+
+
+def test_stop_rules():
+    from psim_gb300 import surrogate as sg
+    r = sg.StopRule.parse("200,10,3.5,2")
+    assert r == sg.StopRule(200, 10, 3.5, 2, 0.0, 0)
+    assert sg.StopRule.parse("50,5,3,3,2.5,50") == sg.StopRule(50, 5, 3.0, 3, 2.5, 50)
+    assert r.detector() == {"window": 200, "batches": 10, "z": 3.5, "patience": 2, "drift_z": 0.0}
+    # checked every patience + 1 windows unless told otherwise
+    assert r.describe().endswith("checked every 600 steps")
+    assert sg.STOP_WARM.describe().endswith("checked every 50 steps")
+    # each rule's shortest stop fits the evaluation runs
+    for rule in (sg.STOP_COLD, sg.STOP_WARM):
+        assert (rule.patience + 1) * rule.window <= 6000 and rule.window % rule.batches == 0
 
 
 @pytest.mark.gpu
