@@ -103,7 +103,8 @@ class StopRule:
 # The steady stops of the evaluation's runs, one for each kind of start.  Both stop runs that are
 # within 3 SE of the steady state (window standard) about 65 % of the time on 512 held-out
 # rectangles: a warm run, which starts close to its steady state, can be stopped by shorter
-# windows at the same accuracy.  Each is its kind's fastest rule of a grid at that accuracy.
+# windows at the same accuracy.  STOP_WARM is the warm runs' fastest rule of a grid at that
+# accuracy; STOP_COLD is within 1 % of the cold runs' fastest.
 STOP_COLD = StopRule(200, 10, 3.5, 2, 0.0, 200)
 STOP_WARM = StopRule(50, 5, 3.0, 3, 0.0, 50)
 
