@@ -487,8 +487,8 @@ def main():
                                      device_queue=bool(opt.device_queue), per_thread=opt.per_thread)
             secs += s_c
             steps_b += n_c
-            # the same models the other way (the autotuner's pilot is a few models; the device queue
-            # gains with the number of models it can spread over the multiprocessors)
+            # the same models the other way, for comparison (the autotuner decides on up to 64 of
+            # them; the device queue gains with the number of models it can spread over the SMs)
             s_o, n_o = api.batch_run(models, workers=16 if opt.device_queue else opt.workers, max_blocks=opt.max_blocks,
                                      device_queue=not bool(opt.device_queue), per_thread=opt.per_thread)
             other_secs += s_o

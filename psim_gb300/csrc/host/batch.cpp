@@ -158,36 +158,50 @@ BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, d
     const std::size_t k = std::min<std::size_t>(models.size(), static_cast<std::size_t>(std::max(1, sample)));
     const std::vector<HostModel*> pilot(models.begin(), models.begin() + static_cast<std::ptrdiff_t>(k));
     const int sms = gpu::sm_count();
-    BatchOptions best;
-    double best_r = -1.;
+    auto rate_of = [](const std::vector<HostModel*>& ms, const BatchOptions& o) {
+        const BatchResult r = run_batch(ms, o);
+        return r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;
+    };
+    // the best of each kind on the pilot
+    BatchOptions best_queue;
+    double queue_r = -1.;
     for (const int per_thread : { 4, 8, 16, 32 }) {// batched launches
         BatchOptions o;
         o.workers = 16;
         o.device_queue = 1;
         o.per_thread = per_thread;
-        const BatchResult r = run_batch(pilot, o);
-        const double rate = r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;
-        if (rate > best_r) {
-            best_r = rate;
-            best = o;
+        const double rate = rate_of(pilot, o);
+        if (rate > queue_r) {
+            queue_r = rate;
+            best_queue = o;
         }
     }
+    BatchOptions best_alone;
+    double alone_r = -1.;
     for (const int workers : { 4, 8, 16, 32 }) {// every model on its own
         for (const int div : { 8, 4, 2, 1 }) {
             BatchOptions o;
             o.workers = workers;
             o.device_queue = 0;
             o.max_blocks = std::max(1, sms / div);
-            const BatchResult r = run_batch(pilot, o);
-            const double rate = r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;
-            if (rate > best_r) {
-                best_r = rate;
-                best = o;
+            const double rate = rate_of(pilot, o);
+            if (rate > alone_r) {
+                alone_r = rate;
+                best_alone = o;
             }
         }
     }
-    if (best_rate != nullptr) { *best_rate = best_r; }
-    return best;
+    // The batched launches gain with the number of models they spread over the multiprocessors, so
+    // a pilot of a few models can favour the other kind: the two finalists run again on up to four
+    // times as many of the batch's models.
+    const std::size_t k2 = std::min<std::size_t>(models.size(), 4U * k);
+    if (k2 > k) {
+        const std::vector<HostModel*> wider(models.begin(), models.begin() + static_cast<std::ptrdiff_t>(k2));
+        queue_r = rate_of(wider, best_queue);
+        alone_r = rate_of(wider, best_alone);
+    }
+    if (best_rate != nullptr) { *best_rate = std::max(queue_r, alone_r); }
+    return queue_r >= alone_r ? best_queue : best_alone;
 }
 
 }// namespace psim

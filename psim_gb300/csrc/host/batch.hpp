@@ -37,7 +37,8 @@ BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions&
 // The autotuner: times the batch's first `sample` models (full runs) under each candidate and
 // returns the fastest, by phonon-steps per second: batched launches with 4, 8, 16 or 32 phonons
 // per thread in a work item, and models on their own under workers {4, 8, 16, 32} x blocks per
-// launch {1/8, 1/4, 1/2, 1} of the multiprocessors.
+// launch {1/8, 1/4, 1/2, 1} of the multiprocessors.  The fastest of each kind then runs again on
+// up to 4 x `sample` of the batch's models, and the faster of the two is returned.
 BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, double* best_rate);
 
 }// namespace psim
