@@ -606,8 +606,7 @@ __device__ __forceinline__ std::uint32_t lanes_run(const StepParams& P, std::uin
             const int lane = static_cast<int>(threadIdx.x & 31U);
             std::uint32_t out_base = 0;
             if (lane == 0 && out_mask != 0U) { out_base = atomicAdd(P.count_out, static_cast<std::uint32_t>(__popc(out_mask))); }
-            cross_add_warp(P, g_smem, crossing, L.step() - P.step);
-            window_add(P, g_smem, crossing, o.tallied, L.step() - P.step, o.sensor, meta_sign(L.p.meta), o.fx, o.fy, false);
+            window_add(P, g_smem, crossing, o.tallied, L.step() - P.step, o.sensor, meta_sign(L.p.meta), o.fx, o.fy);
             if (stays) { lane_enter_step(P, L, L.step() + 1U); }
             out_base = __shfl_sync(full, out_base, 0);
             if (leaving) {

@@ -128,46 +128,26 @@ __device__ __forceinline__ BlockTally window_tally(const StepParams& P, unsigned
 // own: at a few crossings per warp and iteration spread over the sensors, plain shared-memory
 // atomics cost less than grouping the lanes first (__match_any_sync every iteration).
 // 'smem' is the kernel's dynamic shared memory; the tally sits at P.off_tally in it.
-// With count_cross false the caller has counted the crossing already (cross_add_warp).
 __device__ __forceinline__ void window_add(const StepParams& P, unsigned char* smem, bool crossing, bool tallied, std::uint32_t j,
-                                           std::uint32_t sensor, int sign, long long fx, long long fy, bool count_cross = true) {
+                                           std::uint32_t sensor, int sign, long long fx, long long fy) {
     if (!crossing) { return; }
     const BlockTally bt = window_tally(P, smem);
     if (bt.shared) {
         const std::uint32_t i = j * P.n_sensors + sensor;
-        if (count_cross) { atomicAdd(bt.cross() + j, 1U); }
+        atomicAdd(bt.cross() + j, 1U);
         if (tallied) {
             atomicAdd(bt.count() + i, sign);
             atomicAdd(reinterpret_cast<unsigned long long*>(bt.fx() + i), static_cast<unsigned long long>(fx));
             atomicAdd(reinterpret_cast<unsigned long long*>(bt.fy() + i), static_cast<unsigned long long>(fy));
         }
     } else {// tallies straight to global memory; the crossings are still counted per block
-        if (count_cross) { atomicAdd(bt.cross() + j, 1U); }
+        atomicAdd(bt.cross() + j, 1U);
         if (tallied) {
             TallySlot* t = P.tally + static_cast<std::size_t>(P.step + j + 1U - P.step_adj) * P.n_sensors + sensor;
             atomicAdd(reinterpret_cast<unsigned long long*>(&t->count), static_cast<unsigned long long>(static_cast<long long>(sign)));
             atomicAdd(reinterpret_cast<unsigned long long*>(&t->fx), static_cast<unsigned long long>(fx));
             atomicAdd(reinterpret_cast<unsigned long long*>(&t->fy), static_cast<unsigned long long>(fy));
         }
-    }
-}
-
-// Counts the warp's crossings into the launch's steps (step P.step + j + 1 for a lane's j): the
-// lanes crossing into the same step as the first crossing lane add together in one atomic, the
-// others one by one.  Most crossing lanes of an iteration enter the same step, and a same-address
-// shared-memory atomic from many lanes is replayed once per lane.  Called by the whole warp.
-__device__ __forceinline__ void cross_add_warp(const StepParams& P, unsigned char* smem, bool crossing, std::uint32_t j) {
-    const unsigned full = 0xFFFFFFFFU;
-    const unsigned m = __ballot_sync(full, crossing);
-    if (m == 0U) { return; }
-    const int leader = __ffs(static_cast<int>(m)) - 1;
-    const std::uint32_t jl = __shfl_sync(full, j, leader);
-    const unsigned same = __ballot_sync(full, crossing && j == jl);
-    const BlockTally bt = window_tally(P, smem);
-    if (static_cast<int>(threadIdx.x & 31U) == leader) {
-        atomicAdd(bt.cross() + jl, static_cast<std::uint32_t>(__popc(same)));
-    } else if (crossing && j != jl) {
-        atomicAdd(bt.cross() + j, 1U);
     }
 }
 
