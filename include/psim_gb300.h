@@ -169,10 +169,10 @@ typedef struct psim_batch_options {
  * seconds (may be NULL): wall time; phonon_steps (may be NULL): over all models. */
 int psim_batch_run(psim_model* const* models, int32_t n, const psim_batch_options* opt, double* seconds,
                    uint64_t* phonon_steps);
-/* The autotuner: runs the first `sample` models under each candidate (batched launches with 4, 8,
- * 16 or 32 phonons per thread in a work item; models on their own under workers 4, 8, 16, 32 x
- * blocks per launch 1/8, 1/4, 1/2 and all of the multiprocessors), runs the fastest of each kind
- * again on up to 4 x `sample` of the models, and returns the faster of the two and its rate
+/* The autotuner: models on their own under workers 4, 8, 16, 32 x blocks per launch 1/8, 1/4, 1/2
+ * and all of the multiprocessors, timed on the first `sample` models, the fastest of them again on
+ * up to 4 x `sample` models; batched launches with 4, 8, 16 or 32 phonons per thread in a work
+ * item, timed on those 4 x `sample` models.  Returns the fastest options and their rate
  * (phonon-steps/s; may be NULL). */
 int psim_batch_autotune(psim_model* const* models, int32_t n, int32_t sample, psim_batch_options* out,
                         double* best_rate);

@@ -157,25 +157,16 @@ BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, d
     if (models.empty()) { throw std::invalid_argument("empty batch"); }
     const std::size_t k = std::min<std::size_t>(models.size(), static_cast<std::size_t>(std::max(1, sample)));
     const std::vector<HostModel*> pilot(models.begin(), models.begin() + static_cast<std::ptrdiff_t>(k));
+    // The batched launches gain with the number of models they spread over the multiprocessors,
+    // and a few models favour small work items that a large batch does not need: they are timed
+    // on up to four times the pilot's models, against the best worker-thread options of the pilot.
+    const std::size_t k2 = std::min<std::size_t>(models.size(), 4U * k);
+    const std::vector<HostModel*> wider(models.begin(), models.begin() + static_cast<std::ptrdiff_t>(k2));
     const int sms = gpu::sm_count();
     auto rate_of = [](const std::vector<HostModel*>& ms, const BatchOptions& o) {
         const BatchResult r = run_batch(ms, o);
         return r.seconds > 0. ? static_cast<double>(r.phonon_steps) / r.seconds : 0.;
     };
-    // the best of each kind on the pilot
-    BatchOptions best_queue;
-    double queue_r = -1.;
-    for (const int per_thread : { 4, 8, 16, 32 }) {// batched launches
-        BatchOptions o;
-        o.workers = 16;
-        o.device_queue = 1;
-        o.per_thread = per_thread;
-        const double rate = rate_of(pilot, o);
-        if (rate > queue_r) {
-            queue_r = rate;
-            best_queue = o;
-        }
-    }
     BatchOptions best_alone;
     double alone_r = -1.;
     for (const int workers : { 4, 8, 16, 32 }) {// every model on its own
@@ -191,14 +182,19 @@ BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, d
             }
         }
     }
-    // The batched launches gain with the number of models they spread over the multiprocessors, so
-    // a pilot of a few models can favour the other kind: the two finalists run again on up to four
-    // times as many of the batch's models.
-    const std::size_t k2 = std::min<std::size_t>(models.size(), 4U * k);
-    if (k2 > k) {
-        const std::vector<HostModel*> wider(models.begin(), models.begin() + static_cast<std::ptrdiff_t>(k2));
-        queue_r = rate_of(wider, best_queue);
-        alone_r = rate_of(wider, best_alone);
+    if (k2 > k) { alone_r = rate_of(wider, best_alone); }
+    BatchOptions best_queue;
+    double queue_r = -1.;
+    for (const int per_thread : { 4, 8, 16, 32 }) {// batched launches
+        BatchOptions o;
+        o.workers = 16;
+        o.device_queue = 1;
+        o.per_thread = per_thread;
+        const double rate = rate_of(wider, o);
+        if (rate > queue_r) {
+            queue_r = rate;
+            best_queue = o;
+        }
     }
     if (best_rate != nullptr) { *best_rate = std::max(queue_r, alone_r); }
     return queue_r >= alone_r ? best_queue : best_alone;

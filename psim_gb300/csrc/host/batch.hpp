@@ -34,11 +34,11 @@ struct BatchResult {
 // Throws the first failure after every worker has stopped.
 BatchResult run_batch(const std::vector<HostModel*>& models, const BatchOptions& opt);
 
-// The autotuner: times the batch's first `sample` models (full runs) under each candidate and
-// returns the fastest, by phonon-steps per second: batched launches with 4, 8, 16 or 32 phonons
-// per thread in a work item, and models on their own under workers {4, 8, 16, 32} x blocks per
-// launch {1/8, 1/4, 1/2, 1} of the multiprocessors.  The fastest of each kind then runs again on
-// up to 4 x `sample` of the batch's models, and the faster of the two is returned.
+// The autotuner: models on their own under workers {4, 8, 16, 32} x blocks per launch {1/8, 1/4,
+// 1/2, 1} of the multiprocessors, timed on the batch's first `sample` models (full runs), the
+// fastest of them again on up to 4 x `sample` models; batched launches with 4, 8, 16 or 32 phonons
+// per thread in a work item, timed on those 4 x `sample` models.  Returns the fastest, by
+// phonon-steps per second.
 BatchOptions autotune_batch(const std::vector<HostModel*>& models, int sample, double* best_rate);
 
 }// namespace psim
