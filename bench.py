@@ -517,7 +517,8 @@ def main():
                              "1e4-1e6 phonons per step (log-uniform), ends U(280, 320) K, walls U(0, 1) specular; "
                              f"3000 steps of 5 ps, steady state; {min(BATCH_CHUNK, args.batch_models)} alive at once",
                  "autotuned": {"device_queue": opt.device_queue, "per_thread": opt.per_thread, "workers": opt.workers,
-                               "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": min(16, args.batch_models)},
+                               "max_blocks": opt.max_blocks, "pilot_rate": tuned_rate, "pilot_models": min(16, args.batch_models),
+                               "wider_models": min(64, args.batch_models)},
                  "autotuned_value": steps_b / secs, "unit": "phonon-steps/s",
                  "other_mode": {"device_queue": not bool(opt.device_queue), "value": other_steps / other_secs,
                                 "seconds": other_secs},
