@@ -96,6 +96,8 @@ class StopRule:
     def parse(text: str) -> "StopRule":
         """'window,batches,z,patience[,drift_z[,every]]'."""
         f = text.split(",")
+        if not 4 <= len(f) <= 6:
+            raise ValueError(f"a stop rule is window,batches,z,patience[,drift_z[,every]], not {text!r}")
         return StopRule(int(f[0]), int(f[1]), float(f[2]), int(f[3]), float(f[4]) if len(f) > 4 else 0.0,
                         int(f[5]) if len(f) > 5 else 0)
 

@@ -87,6 +87,8 @@ def test_stop_rules():
     assert r == sg.StopRule(200, 10, 3.5, 2, 0.0, 0)
     assert sg.StopRule.parse("50,5,3,3,2.5,50") == sg.StopRule(50, 5, 3.0, 3, 2.5, 50)
     assert r.detector() == {"window": 200, "batches": 10, "z": 3.5, "patience": 2, "drift_z": 0.0}
+    with pytest.raises(ValueError):
+        sg.StopRule.parse("200,10,3.5")
     # checked every patience + 1 windows unless told otherwise
     assert r.describe().endswith("checked every 600 steps")
     assert sg.STOP_WARM.describe().endswith("checked every 50 steps")
