@@ -417,6 +417,10 @@ def main():
         tr = json.load(open(profile))
         roofline["traffic"] = tr.get("dram_bytes_per_phonon_step", 0) * phonon_steps / transport_launches
         roofline["traffic_source"] = tr.get("source")
+        if "issue_active_pct" in tr:  # the bound that holds: instruction issue, from the same kernel's capture
+            roofline["issue_slot_utilisation"] = tr["issue_active_pct"] / 100.0
+            roofline["lanes_per_instruction"] = tr.get("lanes_per_instruction")
+            roofline["issue_source"] = tr.get("issue_source")
 
     # time to steady state of the last timed run (a cold start: every cell at T_ref), by the
     # detector on its device tallies; outside the timed region
