@@ -270,7 +270,18 @@ def summarize_extras(steady, fp64_check, batch, warm, others) -> dict:
     if others is not None:
         out["other_workloads"] = {k: {"value": v["value"], "e2e": v["e2e"], "precision": v["precision"],
                                       "cpu": (v.get("cpu_oracle") or {}).get("value")} for k, v in others.items()}
-    return out
+    return _rounded(out)
+
+
+def _rounded(x, digits: int = 4):
+    """Floats to `digits` significant digits (the full values are on the detail lines)."""
+    if isinstance(x, float):
+        return float(f"{x:.{digits}g}")
+    if isinstance(x, dict):
+        return {k: _rounded(v, digits) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_rounded(v, digits) for v in x]
+    return x
 
 
 def workload_name(args) -> str:

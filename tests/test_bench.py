@@ -94,6 +94,8 @@ def test_extras_summary_is_short_and_keeps_each_measurement():
     assert ex["warm_start"]["steps_ratio_cold_over_warm"] == 4.0 and "per_model" not in ex["warm_start"]
     assert ex["other_workloads"]["bar"] == {"value": 1e10, "e2e": 5e9, "precision": "fp64", "cpu": 1e8}
     assert len(json.dumps(ex)) < 1200
+    # floats keep four significant digits on the headline line
+    assert bench.summarize_extras(None, None, {"value": 11231946816.523619}, None, None)["batch"]["value"] == 1.123e10
     assert bench.summarize_extras(None, None, None, None, None) == {}
 
 
